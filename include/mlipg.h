@@ -1,0 +1,141 @@
+/*
+ * mlipg: linearized-MLIP ("gtinv") energy / force / virial evaluation on one
+ * NVIDIA GB300 (sm_103a), as a plain C ABI.
+ *
+ * Drop-in for the LAMMPS path `pair_style mlip_gtinv` +
+ * `pair_coeff * * <mlp.lammps> El1 ... ElN` of the reference package
+ * (quantum-mtl/lammps-mlip-package).  Every entry point below names the
+ * reference interface it replaces (file:line in that package).
+ *
+ * Conventions
+ *  - Every function returns an int status (MLIPG_OK = 0); on failure the
+ *    message is available from mlipg_last_error().  Nothing calls exit().
+ *  - Host arrays are owned by the caller; the library owns grow-only device
+ *    buffers and one CUDA stream per handle.  A handle is not re-entrant:
+ *    use one handle per thread / MPI rank.
+ *  - Positions are in Angstrom, energies in eV, forces in eV/Angstrom;
+ *    the virial is -sum r_ij (x) f_ij in LAMMPS order xx yy zz xy xz yz.
+ */
+#ifndef MLIPG_H_
+#define MLIPG_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mlipg_handle mlipg_handle;
+
+enum mlipg_status {
+  MLIPG_OK = 0,
+  MLIPG_EINVAL = 1,    /* bad argument */
+  MLIPG_EIO = 2,       /* potential file unreadable or malformed */
+  MLIPG_ENOMEM = 3,    /* device or pinned host allocation failed */
+  MLIPG_ECUDA = 4,     /* CUDA runtime error */
+  MLIPG_ENOTSUP = 5,   /* model outside what the kernels support */
+  MLIPG_ECAPACITY = 6, /* neighbour count above the kernel's capacity */
+  MLIPG_ENOGPU = 7,    /* no usable CUDA device */
+  MLIPG_ETIMEDOUT = 8, /* a wait ran past its deadline */
+  MLIPG_EBUSY = 9      /* request queue full / budget exhausted */
+};
+
+enum mlipg_precision {
+  MLIPG_PREC_FP64 = 0, /* every product and sum in FP64 (plain path) */
+  MLIPG_PREC_MIXED = 1 /* FP32 radial/Y_lm/invariant/adjoint products;
+                          FP64 order-parameter sums, force, energy, virial */
+};
+
+/* Message of the last failure on this handle (h may be NULL for failures
+ * of mlipg_create or of calls without a handle; thread-local). */
+const char* mlipg_last_error(const mlipg_handle* h);
+
+/* Reads a potential file (mlp.lammps format) and uploads the model.
+ * Replaces read_potential_file + MLIPModel::initialize
+ * (src/USER-MLIP/mlipkk_potential_parser.cpp:14-105, mlipkk.cpp:27-53,
+ *  called from PairMLIPGtinvKokkos::coeff, pair_mlip_gtinv_kokkos_impl.h:92-144). */
+int mlipg_create(const char* potential_path, int precision, mlipg_handle** out);
+
+/* Releases device memory and the stream.  (~PairMLIPGtinvKokkos,
+ * pair_mlip_gtinv_kokkos_impl.h:60-85) */
+int mlipg_destroy(mlipg_handle* h);
+
+/* Switches between MLIPG_PREC_FP64 and MLIPG_PREC_MIXED. */
+int mlipg_set_precision(mlipg_handle* h, int precision);
+
+/* Elements of the potential file, their masses and the cutoff radius.
+ * (element list / masses: mlipkk_potential_parser.cpp:26-39,100-102;
+ *  cutoff for init_one: pair_mlip_gtinv_kokkos_impl.h:214-221) */
+int mlipg_num_elements(const mlipg_handle* h);
+const char* mlipg_element_name(const mlipg_handle* h, int k);
+double mlipg_element_mass(const mlipg_handle* h, int k);
+double mlipg_cutoff(const mlipg_handle* h);
+
+/* Maps LAMMPS atom types 1..n_lmp_types to file elements by name, exactly
+ * like the trailing arguments of `pair_coeff * * file El1 ... ElN`;
+ * "NULL" leaves a type unhandled.  Unknown names are an error ("No matching
+ * element in Machine Learning Interatomic Potential file"); all-NULL is an
+ * error ("Incorrect args for pair coefficients").
+ * (pair_mlip_gtinv_kokkos_impl.h:146-195) */
+int mlipg_set_type_map(mlipg_handle* h, int n_lmp_types, const char* const* element_names);
+
+/* One force evaluation on LAMMPS host arrays ("neigh full newton on").
+ *   x[nall*3], type[nall] (1-based LAMMPS types), full neighbour list
+ *   inum/ilist/numneigh/firstneigh (entries masked with NEIGHMASK).
+ * Outputs: f[nall*3] is ACCUMULATED (ghost forces included, to be reverse-
+ * communicated as LAMMPS does); *energy and virial[6] are overwritten when
+ * eflag / vflag are non-zero; eatom[nlocal] is accumulated if not NULL.
+ * Replaces PairMLIPGtinvKokkos::compute (pair_mlip_gtinv_kokkos_impl.h:272-406)
+ * with set_structure (:411-599), MLIPModelLMP::compute (mlipkk_lmp.h:145-228),
+ * get_forces (:601-634) and get_stress (mlipkk_lmp.h:942-955). */
+int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double* x, const int* type,
+                  int inum, const int* ilist, const int* numneigh, const int* const* firstneigh,
+                  int eflag, int vflag, double* f, double* energy, double* virial,
+                  double* eatom);
+
+/* Same evaluation on device-resident data, stream-ordered on the handle's
+ * stream (no host synchronisation; capturable in a CUDA graph).
+ *   d_x4[nall]: x, y, z and the element index as a double (< 0: skip);
+ *   d_centers[ncenters]; CSR d_nbr_off[ncenters+1], d_nbr_idx[...];
+ *   d_img (optional, NULL): packed periodic image per pair,
+ *     code = (n1+512) | (n2+512)<<10 | (n3+512)<<20, 0 = no shift, applied
+ *     with the lattice rows d_cell[9*d_center_cell[c]] of the centre's cell;
+ *   d_fold (optional, NULL): atom -> force row (ghost -> owner).
+ *   d_f[nforce*3] accumulated; d_eatom[ncenters] written (optional);
+ *   d_out8: [energy, virial xx yy zz xy xz yz, spare] written.
+ * No counterpart in the reference (its device stages are internal,
+ * mlipkk_lmp.h:145-228); this is the entry used by MD loops and batching. */
+int mlipg_compute_device(mlipg_handle* h, int ncenters, const void* d_x4, const int* d_centers,
+                         const int* d_nbr_off, const int* d_nbr_idx, const int* d_img,
+                         const double* d_cell, const int* d_center_cell, const int* d_fold,
+                         int nb_cap, double* d_f, double* d_eatom, double* d_out8);
+
+/* The handle's CUDA stream (cudaStream_t) for ordering caller work. */
+void* mlipg_stream(mlipg_handle* h);
+
+/* Status bits raised by the last kernel run (neighbour capacity, bad element). */
+int mlipg_device_status(mlipg_handle* h, int* bits);
+
+/* Number of regression coefficients / structural features implied by a
+ * model specification (MLIPPolynomial::get_n_coeffs,
+ * mlipkk_potential_parser.cpp:107-116).  No GPU needed. */
+int mlipg_count_coefficients(int n_types, int model_type, int maxp, int maxl, int gtinv_order,
+                             const int* gtinv_maxl, const int* gtinv_sym, int n_fn,
+                             long long* n_coeffs, long long* n_features);
+
+/* Model sizes: out[0..12] = T, F, L, Lh, n_irreps, n_terms, n_folded_terms,
+ * n_itc, D, n_coeffs, model_type, maxp, max_nonlinear_itc. */
+int mlipg_model_info(const mlipg_handle* h, long long* out13);
+
+/* Flattened model structure for cross-checks: irreps x typecomb list
+ * [irreps, q, tc_0..tc_{q-1}]... and polynomial index [order, f...]...;
+ * returns the number of ints (out may be NULL to query). */
+long mlipg_dump_itc(const mlipg_handle* h, int* out, long cap);
+long mlipg_dump_poly(const mlipg_handle* h, int* out, long cap);
+
+/* Algorithmic FLOPs per atom step for element `elem` with nbar neighbours. */
+double mlipg_flops_per_atom_step(const mlipg_handle* h, int elem, double nbar);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MLIPG_H_ */

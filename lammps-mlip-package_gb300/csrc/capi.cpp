@@ -1,0 +1,534 @@
+// C-ABI boundary of the GB300 MLIP path (declared in include/mlipg.h).
+//
+// The LAMMPS-facing call mlipg_compute mirrors the reference pair style's
+// compute (pair_mlip_gtinv_kokkos_impl.h:272-406): it packs positions and
+// element indices, flattens the full neighbour list into CSR (4 bytes per
+// pair instead of the reference's 36-byte per-pair records,
+// :411-599), runs the fused kernel and returns forces for owned and ghost
+// atoms, the energy and the virial in LAMMPS order (mlipkk_lmp.h:942-955).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mlipg.h"
+#include "kernels.cuh"
+#include "model.hpp"
+
+using namespace mlipg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+constexpr int kNeighMask = 0x3FFFFFFF;  // LAMMPS NEIGHMASK (SBBITS = 30)
+constexpr int kNbCapMax = 2048;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t reserve(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct HostBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t reserve(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    const size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+    cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct mlipg_handle {
+  Model model;
+  int precision = MLIPG_PREC_FP64;
+  std::string err;
+  std::vector<int> type_map;   // LAMMPS type -> element, index 0 unused, -1 = NULL
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  // model tables on the device
+  DevBuf d_terms, d_units, d_unit_off, d_nl, d_nl_off, d_poly, d_poly_off, d_wlin, d_radial;
+  // per-call buffers (grow only)
+  DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_partials, d_status, d_out8;
+  HostBuf h_x4, h_centers, h_off, h_idx, h_f, h_eatom, h_out;
+  int last_status = 0;
+};
+
+static int fail(mlipg_handle* h, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  g_last_error = buf;
+  return code;
+}
+
+static int cuda_fail(mlipg_handle* h, cudaError_t e, const char* what) {
+  return fail(h, e == cudaErrorMemoryAllocation ? MLIPG_ENOMEM : MLIPG_ECUDA, "%s: %s", what,
+              cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, what); \
+  } while (0)
+
+template <typename T>
+static cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
+  cudaError_t e = b.reserve(std::max<size_t>(v.size() * sizeof(T), 16));
+  if (e != cudaSuccess || v.empty()) return e;
+  return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+static int upload_model(mlipg_handle* h) {
+  const Model& M = h->model;
+  std::vector<DeviceUnit> units, nl;
+  std::vector<DevicePoly> poly;
+  std::vector<int> uoff(M.T + 1, 0), noff(M.T + 1, 0), poff(M.T + 1, 0);
+  for (int t = 0; t < M.T; ++t) {
+    const Schedule& S = M.sched[t];
+    uoff[t] = (int)units.size();
+    noff[t] = (int)nl.size();
+    poff[t] = (int)poly.size();
+    units.insert(units.end(), S.units.begin(), S.units.end());
+    nl.insert(nl.end(), S.nl_units.begin(), S.nl_units.end());
+    poly.insert(poly.end(), S.poly.begin(), S.poly.end());
+  }
+  uoff[M.T] = (int)units.size();
+  noff[M.T] = (int)nl.size();
+  poff[M.T] = (int)poly.size();
+  std::vector<double> radial;
+  for (auto& pr : M.pot.params) {
+    radial.push_back(pr.first);
+    radial.push_back(pr.second);
+  }
+  cudaStream_t s = h->stream;
+  CK(upload(h->d_terms, M.cterms, s), "upload terms");
+  CK(upload(h->d_units, units, s), "upload units");
+  CK(upload(h->d_unit_off, uoff, s), "upload unit offsets");
+  CK(upload(h->d_nl, nl, s), "upload nonlinear units");
+  CK(upload(h->d_nl_off, noff, s), "upload nonlinear offsets");
+  CK(upload(h->d_poly, poly, s), "upload polynomial");
+  CK(upload(h->d_poly_off, poff, s), "upload polynomial offsets");
+  CK(upload(h->d_wlin, M.w_lin, s), "upload linear weights");
+  CK(upload(h->d_radial, radial, s), "upload radial parameters");
+  CK(cudaStreamSynchronize(s), "model upload");
+  return MLIPG_OK;
+}
+
+extern "C" {
+
+const char* mlipg_last_error(const mlipg_handle* h) {
+  if (h && !h->err.empty()) return h->err.c_str();
+  return g_last_error.c_str();
+}
+
+int mlipg_create(const char* path, int precision, mlipg_handle** out) {
+  if (!out || !path) return fail(nullptr, MLIPG_EINVAL, "mlipg_create: null argument");
+  *out = nullptr;
+  if (precision != MLIPG_PREC_FP64 && precision != MLIPG_PREC_MIXED)
+    return fail(nullptr, MLIPG_EINVAL, "unknown precision %d", precision);
+  mlipg_handle* h = new mlipg_handle();
+  h->precision = precision;
+  std::string err;
+  if (!read_potential(path, h->model.pot, err)) {
+    g_last_error = err;
+    delete h;
+    return MLIPG_EIO;
+  }
+  if (!build_model(h->model, err)) {
+    g_last_error = err;
+    delete h;
+    return MLIPG_ENOTSUP;
+  }
+  // default type map: LAMMPS type k -> element k-1
+  h->type_map.assign(h->model.T + 1, -1);
+  for (int k = 1; k <= h->model.T; ++k) h->type_map[k] = k - 1;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    // host-only handle: the model is parsed and queryable; every compute
+    // call fails with MLIPG_ENOGPU
+    cudaGetLastError();
+    h->device = -1;
+    *out = h;
+    return MLIPG_OK;
+  }
+  cudaGetDevice(&h->device);
+  cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = init_device_constants();
+  if (e != cudaSuccess) {
+    g_last_error = std::string("CUDA initialisation failed: ") + cudaGetErrorString(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return MLIPG_ECUDA;
+  }
+  int rc = upload_model(h);
+  if (rc != MLIPG_OK) {
+    g_last_error = h->err;
+    mlipg_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return MLIPG_OK;
+}
+
+int mlipg_destroy(mlipg_handle* h) {
+  if (!h) return MLIPG_OK;
+  if (h->device < 0) {
+    delete h;
+    return MLIPG_OK;
+  }
+  DevBuf* bufs[] = {&h->d_terms, &h->d_units, &h->d_unit_off, &h->d_nl, &h->d_nl_off,
+                    &h->d_poly, &h->d_poly_off, &h->d_wlin, &h->d_radial, &h->d_x4,
+                    &h->d_centers, &h->d_off, &h->d_idx, &h->d_f, &h->d_eatom, &h->d_partials,
+                    &h->d_status, &h->d_out8};
+  for (DevBuf* b : bufs) b->release();
+  HostBuf* hb[] = {&h->h_x4, &h->h_centers, &h->h_off, &h->h_idx, &h->h_f, &h->h_eatom,
+                   &h->h_out};
+  for (HostBuf* b : hb) b->release();
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return MLIPG_OK;
+}
+
+int mlipg_set_precision(mlipg_handle* h, int precision) {
+  if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
+  if (precision != MLIPG_PREC_FP64 && precision != MLIPG_PREC_MIXED)
+    return fail(h, MLIPG_EINVAL, "unknown precision %d", precision);
+  h->precision = precision;
+  return MLIPG_OK;
+}
+
+int mlipg_num_elements(const mlipg_handle* h) { return h ? h->model.T : 0; }
+
+const char* mlipg_element_name(const mlipg_handle* h, int k) {
+  if (!h || k < 0 || k >= h->model.T) return nullptr;
+  return h->model.pot.elements[k].c_str();
+}
+
+double mlipg_element_mass(const mlipg_handle* h, int k) {
+  if (!h || k < 0 || k >= h->model.T) return 0.0;
+  return h->model.pot.masses[k];
+}
+
+double mlipg_cutoff(const mlipg_handle* h) { return h ? h->model.pot.cutoff : 0.0; }
+
+int mlipg_set_type_map(mlipg_handle* h, int n, const char* const* names) {
+  if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
+  if (n < 1 || !names) return fail(h, MLIPG_EINVAL, "Incorrect args for pair coefficients");
+  std::vector<int> map(n + 1, -1);
+  int count = 0;
+  for (int k = 1; k <= n; ++k) {
+    const char* s = names[k - 1];
+    if (!s) return fail(h, MLIPG_EINVAL, "Incorrect args for pair coefficients");
+    if (std::strcmp(s, "NULL") == 0) continue;
+    int j = 0;
+    for (; j < h->model.T; ++j)
+      if (h->model.pot.elements[j] == s) break;
+    if (j == h->model.T)
+      return fail(h, MLIPG_EINVAL,
+                  "No matching element in Machine Learning Interatomic Potential file");
+    map[k] = j;
+    ++count;
+  }
+  if (count == 0) return fail(h, MLIPG_EINVAL, "Incorrect args for pair coefficients");
+  h->type_map = map;
+  return MLIPG_OK;
+}
+
+void* mlipg_stream(mlipg_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int mlipg_device_status(mlipg_handle* h, int* bits) {
+  if (!h || !bits) return fail(h, MLIPG_EINVAL, "null argument");
+  *bits = h->last_status;
+  return MLIPG_OK;
+}
+
+}  // extern "C"
+
+// Launches the fused kernel and the partial-sum reduction on the handle's stream.
+static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const int* centers,
+                      const int* off, const int* idx, const int* img, const double* cell,
+                      const int* center_cell, const int* fold, int nb_cap, double* f,
+                      double* eatom, double* out8) {
+  const Model& M = h->model;
+  const bool fp64 = h->precision == MLIPG_PREC_FP64;
+  nb_cap = std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
+  const int nl_cap = std::max(M.max_nl, 1);
+  const size_t smem = fused_smem_bytes(fp64, M.T, M.Lh, nb_cap, nl_cap);
+  if (smem > 227 * 1024)
+    return fail(h, MLIPG_ENOTSUP,
+                "model needs %zu bytes of shared memory per CTA (limit 232448): "
+                "reduce elements, max_l or radial functions",
+                smem);
+  int bps = fused_max_blocks_per_sm(fp64, M.L, smem);
+  if (bps < 1) return fail(h, MLIPG_ENOTSUP, "fused kernel cannot be resident (smem %zu)", smem);
+  int grid = std::max(1, std::min(ncenters, bps * h->num_sms));
+  CK(h->d_partials.reserve((size_t)grid * 8 * sizeof(double)), "alloc partials");
+  CK(h->d_status.reserve(sizeof(int)), "alloc status");
+  CK(cudaMemsetAsync(h->d_status.p, 0, sizeof(int), h->stream), "memset status");
+  KernelArgs a{};
+  a.x4 = x4;
+  a.centers = centers;
+  a.nbr_off = off;
+  a.nbr_idx = idx;
+  a.img = img;
+  a.cell = cell;
+  a.center_cell = center_cell;
+  a.fold = fold;
+  a.ncenters = ncenters;
+  a.terms = h->d_terms.as<DeviceTerm>();
+  a.units = h->d_units.as<DeviceUnit>();
+  a.unit_off = h->d_unit_off.as<int>();
+  a.nl_units = h->d_nl.as<DeviceUnit>();
+  a.nl_off = h->d_nl_off.as<int>();
+  a.poly = h->d_poly.as<DevicePoly>();
+  a.poly_off = h->d_poly_off.as<int>();
+  a.w_lin = h->d_wlin.as<double>();
+  a.radial = h->d_radial.as<double>();
+  a.T = M.T;
+  a.F = M.F;
+  a.L = M.L;
+  a.Lh = M.Lh;
+  a.nb_cap = nb_cap;
+  a.nl_cap = nl_cap;
+  a.rc = M.pot.cutoff;
+  a.f = f;
+  a.eatom = eatom;
+  a.partials = h->d_partials.as<double>();
+  a.status = h->d_status.as<int>();
+  if (ncenters > 0) CK(launch_fused(fp64, M.L, a, grid, smem, h->stream), "fused kernel launch");
+  else CK(cudaMemsetAsync(a.partials, 0, 8 * sizeof(double), h->stream), "memset partials");
+  CK(launch_finalize(a.partials, ncenters > 0 ? grid : 1, out8, h->stream), "finalize launch");
+  return MLIPG_OK;
+}
+
+extern "C" int mlipg_compute_device(mlipg_handle* h, int ncenters, const void* d_x4,
+                                    const int* d_centers, const int* d_nbr_off,
+                                    const int* d_nbr_idx, const int* d_img, const double* d_cell,
+                                    const int* d_center_cell, const int* d_fold, int nb_cap,
+                                    double* d_f, double* d_eatom, double* d_out8) {
+  if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
+  if (h->device < 0) return fail(h, MLIPG_ENOGPU, "no CUDA device is available");
+  if (ncenters < 0 || (ncenters > 0 && (!d_x4 || !d_centers || !d_nbr_off || !d_nbr_idx)) ||
+      !d_f || !d_out8)
+    return fail(h, MLIPG_EINVAL, "mlipg_compute_device: invalid arguments");
+  if (d_img && (!d_cell || !d_center_cell))
+    return fail(h, MLIPG_EINVAL, "image codes need the cell lattices and centre cell ids");
+  return run_kernel(h, ncenters, static_cast<const double4*>(d_x4), d_centers, d_nbr_off,
+                    d_nbr_idx, d_img, d_cell, d_center_cell, d_fold, nb_cap, d_f, d_eatom,
+                    d_out8);
+}
+
+extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double* x,
+                             const int* type, int inum, const int* ilist, const int* numneigh,
+                             const int* const* firstneigh, int eflag, int vflag, double* f,
+                             double* energy, double* virial, double* eatom) {
+  if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
+  if (h->device < 0) return fail(h, MLIPG_ENOGPU, "no CUDA device is available");
+  if (nlocal < 0 || nall < nlocal || inum < 0 || (nall > 0 && (!x || !type)) ||
+      (inum > 0 && (!ilist || !numneigh || !firstneigh)) || (nall > 0 && !f))
+    return fail(h, MLIPG_EINVAL, "mlipg_compute: invalid arguments");
+  if ((eflag && !energy) || (vflag && !virial))
+    return fail(h, MLIPG_EINVAL, "mlipg_compute: eflag/vflag set without output pointer");
+  const int ntypes = (int)h->type_map.size() - 1;
+  // pack positions and element indices
+  CK(h->h_x4.reserve((size_t)std::max(nall, 1) * sizeof(double4)), "pinned x4");
+  double4* hx = h->h_x4.as<double4>();
+  for (int i = 0; i < nall; ++i) {
+    const int t = type[i];
+    const int e = (t >= 1 && t <= ntypes) ? h->type_map[t] : -1;
+    hx[i] = double4{x[3 * i], x[3 * i + 1], x[3 * i + 2], (double)e};
+  }
+  // centres = owned atoms of ilist; CSR of their full lists
+  CK(h->h_centers.reserve((size_t)std::max(inum, 1) * sizeof(int)), "pinned centres");
+  CK(h->h_off.reserve((size_t)(inum + 1) * sizeof(int)), "pinned offsets");
+  int* hc = h->h_centers.as<int>();
+  int* ho = h->h_off.as<int>();
+  int nc = 0, maxn = 0;
+  long long np = 0;
+  ho[0] = 0;
+  for (int ii = 0; ii < inum; ++ii) {
+    const int i = ilist[ii];
+    if (i < 0 || i >= nlocal) continue;
+    hc[nc] = i;
+    np += numneigh[i];
+    maxn = std::max(maxn, numneigh[i]);
+    if (np > 2147483647LL) return fail(h, MLIPG_EINVAL, "more than 2^31 neighbour pairs");
+    ho[nc + 1] = (int)np;
+    ++nc;
+  }
+  CK(h->h_idx.reserve((size_t)std::max<long long>(np, 1) * sizeof(int)), "pinned neighbours");
+  int* hi = h->h_idx.as<int>();
+  for (int c = 0; c < nc; ++c) {
+    const int i = hc[c];
+    const int* jl = firstneigh[i];
+    int* dst = hi + ho[c];
+    for (int jj = 0; jj < numneigh[i]; ++jj) {
+      const int j = jl[jj] & kNeighMask;
+      if (j < 0 || j >= nall) return fail(h, MLIPG_EINVAL, "neighbour index %d outside nall", j);
+      dst[jj] = j;
+    }
+  }
+  // upload
+  cudaStream_t s = h->stream;
+  CK(h->d_x4.reserve((size_t)std::max(nall, 1) * sizeof(double4)), "alloc x4");
+  CK(h->d_centers.reserve((size_t)std::max(nc, 1) * sizeof(int)), "alloc centres");
+  CK(h->d_off.reserve((size_t)(nc + 1) * sizeof(int)), "alloc offsets");
+  CK(h->d_idx.reserve((size_t)std::max<long long>(np, 1) * sizeof(int)), "alloc neighbours");
+  CK(h->d_f.reserve((size_t)std::max(nall, 1) * 3 * sizeof(double)), "alloc forces");
+  CK(h->d_eatom.reserve((size_t)std::max(nc, 1) * sizeof(double)), "alloc eatom");
+  CK(h->d_out8.reserve(8 * sizeof(double)), "alloc out");
+  CK(cudaMemcpyAsync(h->d_x4.p, hx, (size_t)nall * sizeof(double4), cudaMemcpyHostToDevice, s),
+     "copy x4");
+  CK(cudaMemcpyAsync(h->d_centers.p, hc, (size_t)nc * sizeof(int), cudaMemcpyHostToDevice, s),
+     "copy centres");
+  CK(cudaMemcpyAsync(h->d_off.p, ho, (size_t)(nc + 1) * sizeof(int), cudaMemcpyHostToDevice, s),
+     "copy offsets");
+  if (np > 0)
+    CK(cudaMemcpyAsync(h->d_idx.p, hi, (size_t)np * sizeof(int), cudaMemcpyHostToDevice, s),
+       "copy neighbours");
+  CK(cudaMemsetAsync(h->d_f.p, 0, (size_t)nall * 3 * sizeof(double), s), "memset forces");
+  int rc = run_kernel(h, nc, h->d_x4.as<double4>(), h->d_centers.as<int>(), h->d_off.as<int>(),
+                      h->d_idx.as<int>(), nullptr, nullptr, nullptr, nullptr, maxn,
+                      h->d_f.as<double>(), h->d_eatom.as<double>(), h->d_out8.as<double>());
+  if (rc != MLIPG_OK) return rc;
+  // download
+  CK(h->h_f.reserve((size_t)std::max(nall, 1) * 3 * sizeof(double)), "pinned forces");
+  CK(h->h_eatom.reserve((size_t)std::max(nc, 1) * sizeof(double)), "pinned eatom");
+  CK(h->h_out.reserve(16 * sizeof(double)), "pinned out");
+  CK(cudaMemcpyAsync(h->h_f.p, h->d_f.p, (size_t)nall * 3 * sizeof(double),
+                     cudaMemcpyDeviceToHost, s),
+     "copy forces");
+  if (eatom)
+    CK(cudaMemcpyAsync(h->h_eatom.p, h->d_eatom.p, (size_t)nc * sizeof(double),
+                       cudaMemcpyDeviceToHost, s),
+       "copy eatom");
+  CK(cudaMemcpyAsync(h->h_out.p, h->d_out8.p, 8 * sizeof(double), cudaMemcpyDeviceToHost, s),
+     "copy energy");
+  CK(cudaMemcpyAsync(h->h_out.as<double>() + 8, h->d_status.p, sizeof(int),
+                     cudaMemcpyDeviceToHost, s),
+     "copy status");
+  CK(cudaStreamSynchronize(s), "mlipg_compute");
+  int status = 0;
+  std::memcpy(&status, h->h_out.as<double>() + 8, sizeof(int));
+  h->last_status = status;
+  if (status & kStatusNeighbourCapacity)
+    return fail(h, MLIPG_ECAPACITY, "an atom has more than %d neighbours inside the cutoff",
+                std::max(32, std::min(kNbCapMax, (maxn + 31) / 32 * 32)));
+  if (status & kStatusBadType) return fail(h, MLIPG_EINVAL, "element index out of range");
+  const double* hf = h->h_f.as<double>();
+  for (size_t k = 0; k < (size_t)nall * 3; ++k) f[k] += hf[k];
+  const double* o = h->h_out.as<double>();
+  if (eflag) *energy = o[0];
+  if (vflag) {
+    // kernel order xx yy zz yz zx xy -> LAMMPS xx yy zz xy xz yz
+    virial[0] = o[1];
+    virial[1] = o[2];
+    virial[2] = o[3];
+    virial[3] = o[6];
+    virial[4] = o[5];
+    virial[5] = o[4];
+  }
+  if (eatom) {
+    const double* he = h->h_eatom.as<double>();
+    for (int c = 0; c < nc; ++c) eatom[hc[c]] += he[c];
+  }
+  return MLIPG_OK;
+}
+
+extern "C" int mlipg_count_coefficients(int n_types, int model_type, int maxp, int maxl,
+                                        int gtinv_order, const int* gtinv_maxl,
+                                        const int* gtinv_sym, int n_fn, long long* n_coeffs,
+                                        long long* n_features) {
+  if (!n_coeffs || !n_features || (gtinv_order > 1 && (!gtinv_maxl || !gtinv_sym)))
+    return fail(nullptr, MLIPG_EINVAL, "mlipg_count_coefficients: null argument");
+  std::string err;
+  if (!count_coefficients(n_types, model_type, maxp, maxl, gtinv_order, gtinv_maxl, gtinv_sym,
+                          n_fn, n_coeffs, n_features, err))
+    return fail(nullptr, MLIPG_EINVAL, "%s", err.c_str());
+  return MLIPG_OK;
+}
+
+extern "C" int mlipg_model_info(const mlipg_handle* h, long long* out) {
+  if (!h || !out) return fail(nullptr, MLIPG_EINVAL, "null argument");
+  const Model& M = h->model;
+  long long v[13] = {M.T, M.F, M.L, M.Lh, (long long)M.irr_l.size(), (long long)M.term_c.size(),
+                     (long long)M.cterms.size(), M.n_itc, M.D, (long long)M.poly.size(),
+                     M.pot.model_type, M.pot.maxp, M.max_nl};
+  std::memcpy(out, v, sizeof v);
+  return MLIPG_OK;
+}
+
+extern "C" long mlipg_dump_itc(const mlipg_handle* h, int* out, long cap) {
+  if (!h) return -1;
+  long k = 0;
+  for (auto& x : h->model.itc) {
+    const long q = (long)x.type_combs.size();
+    if (out && k + 2 + q <= cap) {
+      out[k] = x.irreps;
+      out[k + 1] = (int)q;
+      for (long p = 0; p < q; ++p) out[k + 2 + p] = x.type_combs[p];
+    }
+    k += 2 + q;
+  }
+  return k;
+}
+
+extern "C" long mlipg_dump_poly(const mlipg_handle* h, int* out, long cap) {
+  if (!h) return -1;
+  long k = 0;
+  for (auto& row : h->model.poly) {
+    const long q = (long)row.size();
+    if (out && k + 1 + q <= cap) {
+      out[k] = (int)q;
+      for (long p = 0; p < q; ++p) out[k + 1 + p] = row[p];
+    }
+    k += 1 + q;
+  }
+  return k;
+}
+
+extern "C" double mlipg_flops_per_atom_step(const mlipg_handle* h, int elem, double nbar) {
+  if (!h || elem < 0 || elem >= h->model.T) return 0.0;
+  return flops_per_atom_step(h->model, elem, nbar);
+}

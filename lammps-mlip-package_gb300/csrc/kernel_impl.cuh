@@ -1,0 +1,698 @@
+// Fused per-atom MLIP kernel, included once per arithmetic precision.
+//
+// One CTA evaluates one centre atom at a time (persistent grid-stride loop
+// over centres); every intermediate of the reference's seven stages stays in
+// shared memory:
+//   P1  neighbour compaction: keep r <= rc, stable-sort by element (warp 0)
+//   P2  order parameters a[s][lm][n] = sum_j f_n(r) conj(Y_lm), products in
+//       REAL, sums in FP64 (mlipkk_lmp.h:314-387, mlipkk_features_kk.h:9-48,
+//       mlipkk_spherical_harmonics_kk.h:18-81)
+//   P3  nonlinear features and polynomial terms of order >= 2: energy part
+//       and H = dE/dd for those features (mlipkk_lmp.h:489-625)
+//   P5  invariants d over the folded coupling table, linear energy
+//       sum w_f d_f, and G = dE/da via H (mlipkk_lmp.h:407-469, 645-733)
+//   P6  per-pair forces f_ij = sum coeff Re(G . dphi*) with the centre's own
+//       adjoint, scattered as F_i += f, F_j -= f; virial -= r_ij (x) f
+//       (mlipkk_lmp.h:753-922, spherical-harmonic derivatives :117-177)
+// The "owner computes" force form: a pair's other half comes from the
+// neighbour's own evaluation (identical to the reference's j<i / ghost
+// split up to summation order).
+//
+// Required macros: MLIPG_REAL (float|double), MLIPG_TAG (f32|f64).
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.cuh"
+
+#define MLIPG_CAT2(a, b) a##b
+#define MLIPG_CAT(a, b) MLIPG_CAT2(a, b)
+
+namespace mlipg {
+namespace MLIPG_TAG {
+
+using R = MLIPG_REAL;
+template <typename T> struct Cx;
+template <> struct Cx<float> { using type = float2; };
+template <> struct Cx<double> { using type = double2; };
+using Rc = Cx<R>::type;
+
+namespace {
+
+// spherical-harmonic recursion constants (mlipkk.cpp:247-272 and
+// mlipkk_spherical_harmonics_kk.h), indexed by lm2i(l, m) = l(l+1)/2 + m
+__constant__ R cA[kLhMax];
+__constant__ R cB[kLhMax];
+__constant__ R cLM[kLhMax];        // sqrt((l-m)(l+m+1))
+__constant__ R cDiag[kMaxL + 2];   // -sqrt(1 + 0.5/m), m >= 1
+__constant__ R cOff[kMaxL + 2];    // sqrt(2m + 3)
+__constant__ R cLL[kMaxL + 1];     // sqrt(0.5 l (l+1))
+
+__device__ __forceinline__ int lm2i(int l, int m) { return l * (l + 1) / 2 + m; }
+
+__device__ __forceinline__ float rsqrt_r(float v) { return rsqrtf(v); }
+__device__ __forceinline__ double rsqrt_r(double v) { return 1.0 / sqrt(v); }
+
+__device__ __forceinline__ R exp_r(R v) { return exp(v); }
+__device__ __forceinline__ void sincospi_r(R v, R* s, R* c) { sincospi(v, s, c); }
+
+// Visits every (l, m <= 0) with Y_{l,m} and, if DERIV, dY/dx, dY/dy, dY/dz,
+// in the order m = 0, -1, ..., -L (outer) and l = |m|..L (inner).  The
+// associated-Legendre columns are advanced in registers: the recursion of
+// the reference (DLMF 14.10.3 / 14.7.15 with normalised P and Q = P/sin) is
+// the same, evaluated column by column.
+template <int LCAP, bool DERIV, typename V>
+__device__ __forceinline__ void sh_visit(R dx, R dy, R dz, R r, int L, V& vis) {
+  const R invr = R(1) / r;
+  const R ct = dz * invr;
+  const R st = sqrt(fmax(R(0), R(1) - ct * ct));
+  const R rho2 = dx * dx + dy * dy;
+  R cp = R(1), sp = R(0);
+  if (rho2 > R(0)) {
+    const R ir = rsqrt_r(rho2);
+    cp = dx * ir;
+    sp = dy * ir;
+  }
+  const R h = R(0.70710678118654752440);  // 0.5 * sqrt(2)
+  R Qc[LCAP + 2];
+#pragma unroll
+  for (int l = 0; l < LCAP + 2; ++l) Qc[l] = R(0);
+  R pdiag = R(0.39894228040143267794);    // P_0^0 = sqrt(1/(2 pi))
+  R cm = R(1), sm = R(0), cprev = cp, sprev = -sp;
+  const R tc = R(2) * cp;
+  R sgn = R(1);
+#pragma unroll
+  for (int mp = 0; mp <= LCAP; ++mp) {
+    if (mp > L) break;
+    if (mp > 0) {
+      const R s = tc * sm - sprev;
+      const R c = tc * cm - cprev;
+      cprev = cm; cm = c; sprev = sm; sm = s;
+      pdiag = pdiag * (cDiag[mp] * st);
+      sgn = -sgn;
+    }
+    // next Q column (m = mp + 1): diagonal start
+    R qn_diag = R(0);
+    if (DERIV) {
+      qn_diag = (mp == 0) ? R(-0.48860251190291992263) : Qc[mp] * (cDiag[mp + 1] * st);
+    }
+    R p1 = R(0), p2 = R(0), qn1 = R(0), qn2 = R(0);
+#pragma unroll
+    for (int l = mp; l <= LCAP; ++l) {
+      if (l > L) break;
+      R P;
+      if (l == mp) P = pdiag;
+      else if (l == mp + 1) P = (ct * cOff[mp]) * p1;
+      else P = cA[lm2i(l, mp)] * (ct * p1 + cB[lm2i(l, mp)] * p2);
+      p2 = p1;
+      p1 = P;
+      R Qn = R(0);
+      if (DERIV) {
+        if (l == mp + 1) Qn = qn_diag;
+        else if (l == mp + 2) Qn = (ct * cOff[mp + 1]) * qn1;
+        else if (l >= mp + 3) Qn = cA[lm2i(l, mp + 1)] * (ct * qn1 + cB[lm2i(l, mp + 1)] * qn2);
+        if (l >= mp + 1) { qn2 = qn1; qn1 = Qn; }
+      }
+      R yre, yim;
+      if (mp == 0) {
+        yre = P * h;
+        yim = R(0);
+      } else {
+        const R t = sgn * P * h;
+        yre = t * cm;
+        yim = -(t * sm);
+      }
+      const int lmh = l * (l + 1) / 2 + l - mp;
+      if (DERIV) {
+        R xre = 0, xim = 0, yyre = 0, yyim = 0, zre = 0, zim = 0;
+        if (mp == 0) {
+          if (l >= 1) {
+            const R common = Qn * st * invr * cLL[l];
+            xre = common * ct * cp;
+            yyre = common * ct * sp;
+            zre = -common * st;
+          }
+        } else {
+          const R qc = Qc[l];
+          R dth = R(mp) * ct * qc;
+          if (l != mp) dth += cLM[lm2i(l, mp)] * Qn * st;
+          const R dph = R(mp) * qc;
+          const R ere = cm * h * invr, eim = sm * h * invr;
+          // v = (dth ct cp) + i(-dph sp), (dth ct sp) + i(dph cp), (-dth st)
+          const R vxr = dth * ct * cp, vxi = -dph * sp;
+          const R vyr = dth * ct * sp, vyi = dph * cp;
+          const R vzr = -dth * st;
+          xre = sgn * (ere * vxr - eim * vxi);
+          xim = -sgn * (ere * vxi + eim * vxr);
+          yyre = sgn * (ere * vyr - eim * vyi);
+          yyim = -sgn * (ere * vyi + eim * vyr);
+          zre = sgn * (ere * vzr);
+          zim = -sgn * (eim * vzr);
+        }
+        vis(lmh, mp, yre, yim, xre, xim, yyre, yyim, zre, zim);
+        if (l >= mp + 1) Qc[l] = Qn;
+      } else {
+        vis(lmh, mp, yre, yim, R(0), R(0), R(0), R(0), R(0), R(0));
+      }
+    }
+  }
+}
+
+// radial basis: f_n = exp(-beta (r-mu)^2) fc(r), fc = (cos(pi r/rc) + 1)/2
+__device__ __forceinline__ void radial(const double* __restrict__ prm, int F, R r, R rc, R* f,
+                                       R* fd, bool deriv) {
+  R sn, cs;
+  sincospi_r(r / rc, &sn, &cs);
+  const bool in = r < rc;
+  const R fc = in ? R(0.5) * (cs + R(1)) : R(0);
+  const R fcd = in ? R(-0.5) * R(3.14159265358979323846) / rc * sn : R(0);
+#pragma unroll
+  for (int n = 0; n < kNPad; ++n) {
+    if (n < F) {
+      const R beta = (R)__ldg(prm + 2 * n), mu = (R)__ldg(prm + 2 * n + 1);
+      const R dr = r - mu;
+      const R bf = exp_r(-beta * dr * dr);
+      f[n] = bf * fc;
+      if (deriv) fd[n] = (R(-2) * beta * dr * bf) * fc + bf * fcd;
+    } else {
+      f[n] = R(0);
+      if (deriv) fd[n] = R(0);
+    }
+  }
+}
+
+struct StageVis {
+  Rc* ys;
+  int slot;
+  __device__ __forceinline__ void operator()(int lmh, int, R yre, R yim, R, R, R, R, R, R) {
+    ys[lmh * kChunk + slot] = Rc{yre, yim};
+  }
+};
+
+struct ForceVis {
+  const Rc* g;   // G of the neighbour's element slot: [Lh][16]
+  const R* f;
+  const R* fd;
+  int F;
+  R ux, uy, uz;
+  R fx, fy, fz;
+  __device__ __forceinline__ void operator()(int lmh, int mp, R yre, R yim, R xre, R xim, R yyre,
+                                             R yyim, R zre, R zim) {
+    const Rc* gg = g + lmh * kNPad;
+    R g0r = 0, g0i = 0, g1r = 0, g1i = 0;
+#pragma unroll
+    for (int n = 0; n < kNPad; ++n) {
+      if (n < F) {
+        const Rc v = gg[n];
+        g0r += f[n] * v.x;
+        g0i += f[n] * v.y;
+        g1r += fd[n] * v.x;
+        g1i += fd[n] * v.y;
+      }
+    }
+    const R coeff = (mp == 0) ? R(1) : R(2);
+    const R ry = yre * g1r + yim * g1i;
+    fx += coeff * (ry * ux + (xre * g0r + xim * g0i));
+    fy += coeff * (ry * uy + (yyre * g0r + yyim * g0i));
+    fz += coeff * (ry * uz + (zre * g0r + zim * g0i));
+  }
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// displacement x_j - x_i (+ periodic image shift for batched cells)
+__device__ __forceinline__ void pair_disp(const KernelArgs& A, int c, int k, const double4& xi,
+                                          const double4& xj, double& dx, double& dy, double& dz) {
+  dx = xj.x - xi.x;
+  dy = xj.y - xi.y;
+  dz = xj.z - xi.z;
+  if (A.img != nullptr) {
+    const int code = __ldg(A.img + k);
+    if (code != 0) {
+      const double n1 = (double)((code & 1023) - 512);
+      const double n2 = (double)(((code >> 10) & 1023) - 512);
+      const double n3 = (double)(((code >> 20) & 1023) - 512);
+      const double* L = A.cell + 9 * __ldg(A.center_cell + c);
+      dx += n1 * L[0] + n2 * L[3] + n3 * L[6];
+      dy += n1 * L[1] + n2 * L[4] + n3 * L[7];
+      dz += n1 * L[2] + n2 * L[5] + n3 * L[8];
+    }
+  }
+}
+
+// One coupling unit for all n: warp halves take alternate terms.
+template <int Q, bool WITH_G>
+__device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* __restrict__ terms,
+                                         const Rc* sa, Rc* sg, int Lh, int n, int half, bool act,
+                                         R H, R& dsum) {
+  int off[Q];
+#pragma unroll
+  for (int p = 0; p < Q; ++p) off[p] = (int)u.s[p] * Lh * kNPad + n;
+  const int kend = u.term0 + u.nterm;
+  for (int k = u.term0 + half; k < kend; k += 2) {
+    const int4 raw = __ldg(reinterpret_cast<const int4*>(terms + k));
+    const R c = (R)__hiloint2double(raw.y, raw.x);
+    const unsigned lw = (unsigned)raw.z, hw = (unsigned)raw.w;
+    const unsigned code = hw >> 16;
+    int lmh[Q];
+    R ar[Q], ai[Q];
+#pragma unroll
+    for (int p = 0; p < Q; ++p) {
+      lmh[p] = p < 4 ? (int)((lw >> (8 * p)) & 255u) : (int)((hw >> (8 * (p - 4))) & 255u);
+      const Rc v = sa[off[p] + lmh[p] * kNPad];
+      const unsigned cd = (code >> (2 * p)) & 3u;
+      ar[p] = v.x;
+      ai[p] = (cd == (unsigned)kSlotConj) ? -v.y : v.y;
+    }
+    const bool self = (code >> 12) & 1u;
+    // prefix products pr[p] = prod_{p' < p} a~, suffix su[p] = prod_{p' > p} a~
+    R prr[Q], pri[Q], sur[Q], sui[Q];
+    prr[0] = R(1); pri[0] = R(0);
+#pragma unroll
+    for (int p = 1; p < Q; ++p) {
+      if (p == 1) { prr[1] = ar[0]; pri[1] = ai[0]; }
+      else {
+        prr[p] = prr[p - 1] * ar[p - 1] - pri[p - 1] * ai[p - 1];
+        pri[p] = prr[p - 1] * ai[p - 1] + pri[p - 1] * ar[p - 1];
+      }
+    }
+    sur[Q - 1] = R(1); sui[Q - 1] = R(0);
+#pragma unroll
+    for (int p = Q - 2; p >= 0; --p) {
+      if (p == Q - 2) { sur[p] = ar[Q - 1]; sui[p] = ai[Q - 1]; }
+      else {
+        sur[p] = sur[p + 1] * ar[p + 1] - sui[p + 1] * ai[p + 1];
+        sui[p] = sur[p + 1] * ai[p + 1] + sui[p + 1] * ar[p + 1];
+      }
+    }
+    // full product real part
+    const R full = prr[Q - 1] * ar[Q - 1] - pri[Q - 1] * ai[Q - 1];
+    dsum += (self ? c : R(2) * c) * full;
+    if (WITH_G) {
+      const R cc = c * H;
+#pragma unroll
+      for (int p = 0; p < Q; ++p) {
+        R Pr, Pi;
+        if (p == 0) { Pr = sur[0]; Pi = sui[0]; }
+        else if (p == Q - 1) { Pr = prr[Q - 1]; Pi = pri[Q - 1]; }
+        else {
+          Pr = prr[p] * sur[p] - pri[p] * sui[p];
+          Pi = prr[p] * sui[p] + pri[p] * sur[p];
+        }
+        const unsigned cd = (code >> (2 * p)) & 3u;
+        const R kr = (cd == (unsigned)kSlotMZero) ? R(2) : R(1);
+        if (act) {
+          Rc* gp = sg + off[p] + lmh[p] * kNPad;
+          atomicAdd(&gp->x, cc * kr * Pr);
+          if (cd < 2u) atomicAdd(&gp->y, (cd == 0u ? cc : -cc) * Pi);
+        }
+      }
+    }
+  }
+}
+
+template <bool WITH_G>
+__device__ __forceinline__ void dispatch_unit(const DeviceUnit& u, const DeviceTerm* terms,
+                                              const Rc* sa, Rc* sg, int Lh, int n, int half,
+                                              bool act, R H, R& dsum) {
+  switch (u.q) {
+    case 1: run_unit<1, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
+    case 2: run_unit<2, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
+    case 3: run_unit<3, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
+    case 4: run_unit<4, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
+    case 5: run_unit<5, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
+    default: run_unit<6, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
+  }
+}
+
+}  // namespace
+
+__host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+
+struct SmemLayout {
+  size_t a, g, dnl, hnl, nbk, misc, red, total;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int nl_cap) {
+  SmemLayout s;
+  const size_t an = (size_t)T * Lh * kNPad * sizeof(Rc);
+  const size_t stage = (size_t)Lh * kChunk * sizeof(Rc) + (size_t)kChunk * kNPad * sizeof(R);
+  s.a = 0;
+  s.g = align16(an);
+  s.dnl = s.g + align16(an > stage ? an : stage);
+  s.hnl = s.dnl + align16((size_t)nl_cap * kNPad * sizeof(double));
+  s.nbk = s.hnl + align16((size_t)nl_cap * kNPad * sizeof(double));
+  s.misc = s.nbk + align16((size_t)nb_cap * sizeof(int));
+  s.red = s.misc + align16(32 * sizeof(int));
+  s.total = s.red + align16(8 * (kBlock / 32) * sizeof(double));
+  return s;
+}
+
+template <int LCAP>
+__global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ KernelArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int T = A.T, F = A.F, Lh = A.Lh, L = A.L;
+  const SmemLayout lay = smem_layout(T, Lh, A.nb_cap, A.nl_cap);
+  Rc* sa = reinterpret_cast<Rc*>(smem + lay.a);
+  Rc* sg = reinterpret_cast<Rc*>(smem + lay.g);
+  Rc* ys = sg;                                                      // P2 staging
+  R* fs = reinterpret_cast<R*>(smem + lay.g + (size_t)Lh * kChunk * sizeof(Rc));
+  double* dnl = reinterpret_cast<double*>(smem + lay.dnl);
+  double* hnl = reinterpret_cast<double*>(smem + lay.hnl);
+  int* nbk = reinterpret_cast<int*>(smem + lay.nbk);
+  int* misc = reinterpret_cast<int*>(smem + lay.misc);   // [0..8] type offsets, [9] skip, [10] ctr
+  double* red = reinterpret_cast<double*>(smem + lay.red);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const R rc = (R)A.rc;
+  const double rc2 = A.rc * A.rc;
+  constexpr int kLhCap = (LCAP + 1) * (LCAP + 2) / 2;
+  constexpr int kEPT = (kLhCap * kNPad + kBlock - 1) / kBlock;
+
+  double vir[6] = {0, 0, 0, 0, 0, 0};
+  double ecta = 0.0;
+
+  for (int c = blockIdx.x; c < A.ncenters; c += gridDim.x) {
+    const int i = __ldg(A.centers + c);
+    const double4 xi = A.x4[i];
+    const int ti = (int)xi.w;
+    if (ti < 0 || ti >= T) {
+      if (tid == 0) {
+        if (A.eatom) A.eatom[c] = 0.0;
+        if (ti >= T) atomicOr(A.status, kStatusBadType);
+      }
+      continue;
+    }
+    const int o0 = __ldg(A.nbr_off + c), o1 = __ldg(A.nbr_off + c + 1);
+    // ---------------------------------------------------------------- P1
+    if (warp == 0) {
+      int cnt[kMaxTypes];
+#pragma unroll
+      for (int t = 0; t < kMaxTypes; ++t) cnt[t] = 0;
+      for (int base = o0; base < o1; base += 32) {
+        const int k = base + lane;
+        int t = -1;
+        if (k < o1) {
+          const int j = __ldg(A.nbr_idx + k);
+          const double4 xj = A.x4[j];
+          double dx, dy, dz;
+          pair_disp(A, c, k, xi, xj, dx, dy, dz);
+          const double r2 = dx * dx + dy * dy + dz * dz;
+          t = (int)xj.w;
+          if (!(t >= 0 && t < T && r2 <= rc2 && r2 > 0.0)) t = -1;
+        }
+#pragma unroll
+        for (int tt = 0; tt < kMaxTypes; ++tt)
+          if (tt < T) cnt[tt] += __popc(__ballot_sync(0xffffffffu, t == tt));
+      }
+      int tot = 0, toff[kMaxTypes + 1];
+#pragma unroll
+      for (int tt = 0; tt < kMaxTypes; ++tt) {
+        toff[tt] = tot;
+        if (tt < T) tot += cnt[tt];
+      }
+      toff[kMaxTypes] = tot;
+      const bool over = tot > A.nb_cap;
+      if (!over) {
+        int cur[kMaxTypes];
+#pragma unroll
+        for (int tt = 0; tt < kMaxTypes; ++tt) cur[tt] = toff[tt];
+        const unsigned lt = (1u << lane) - 1u;
+        for (int base = o0; base < o1; base += 32) {
+          const int k = base + lane;
+          int t = -1;
+          if (k < o1) {
+            const int j = __ldg(A.nbr_idx + k);
+            const double4 xj = A.x4[j];
+            double dx, dy, dz;
+            pair_disp(A, c, k, xi, xj, dx, dy, dz);
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            t = (int)xj.w;
+            if (!(t >= 0 && t < T && r2 <= rc2 && r2 > 0.0)) t = -1;
+          }
+#pragma unroll
+          for (int tt = 0; tt < kMaxTypes; ++tt) {
+            if (tt < T) {
+              const unsigned b = __ballot_sync(0xffffffffu, t == tt);
+              if (t == tt) nbk[cur[tt] + __popc(b & lt)] = k;
+              cur[tt] += __popc(b);
+            }
+          }
+        }
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int tt = 0; tt <= kMaxTypes; ++tt) misc[tt] = tt < T ? toff[tt] : tot;
+        misc[9] = over ? 1 : 0;
+        misc[10] = 0;
+        if (over) atomicOr(A.status, kStatusNeighbourCapacity);
+      }
+    }
+    __syncthreads();
+    if (misc[9]) {
+      if (tid == 0 && A.eatom) A.eatom[c] = 0.0;
+      __syncthreads();
+      continue;
+    }
+    const int nkeep = misc[T];
+    // ---------------------------------------------------------------- P2
+    for (int t = 0; t < T; ++t) {
+      double accr[kEPT], acci[kEPT];
+#pragma unroll
+      for (int e = 0; e < kEPT; ++e) { accr[e] = 0.0; acci[e] = 0.0; }
+      const int b0 = misc[t], b1 = misc[t + 1];
+      for (int cb = b0; cb < b1; cb += kChunk) {
+        const int csz = min(kChunk, b1 - cb);
+        if (tid < csz) {
+          const int k = nbk[cb + tid];
+          const int j = __ldg(A.nbr_idx + k);
+          double dx, dy, dz;
+          pair_disp(A, c, k, xi, A.x4[j], dx, dy, dz);
+          const double r = sqrt(dx * dx + dy * dy + dz * dz);
+          R f[kNPad], fdum[kNPad];
+          radial(A.radial, F, (R)r, rc, f, fdum, false);
+#pragma unroll
+          for (int n = 0; n < kNPad; ++n) fs[tid * kNPad + n] = f[n];
+          StageVis v{ys, tid};
+          sh_visit<LCAP, false>((R)dx, (R)dy, (R)dz, (R)r, L, v);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < kEPT; ++e) {
+          const int idx = tid + e * kBlock;
+          const int lmh = idx >> 4, n = idx & 15;
+          if (lmh < Lh && n < F) {
+            for (int jj = 0; jj < csz; ++jj) {
+              const R fv = fs[jj * kNPad + n];
+              const Rc y = ys[lmh * kChunk + jj];
+              accr[e] += (double)(fv * y.x);
+              acci[e] -= (double)(fv * y.y);
+            }
+          }
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int e = 0; e < kEPT; ++e) {
+        const int idx = tid + e * kBlock;
+        const int lmh = idx >> 4;
+        if (lmh < Lh) sa[(t * Lh + lmh) * kNPad + (idx & 15)] = Rc{(R)accr[e], (R)acci[e]};
+      }
+    }
+    // ---------------------------------------------------------------- P3
+    double eacc = 0.0;
+    const int nl0 = __ldg(A.nl_off + ti), nNL = __ldg(A.nl_off + ti + 1) - nl0;
+    const int n = lane & 15, half = lane >> 4;
+    const bool act = n < F;
+    if (nNL > 0) {
+      for (int e = tid; e < nNL * kNPad; e += kBlock) hnl[e] = 0.0;
+      __syncthreads();  // a[] complete
+      for (int u = warp; u < nNL; u += kBlock / 32) {
+        const DeviceUnit un = A.nl_units[nl0 + u];
+        R dsum = R(0);
+        dispatch_unit<false>(un, A.terms, sa, sg, Lh, n, half, act, R(0), dsum);
+        dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
+        if (half == 0) dnl[u * kNPad + n] = act ? (double)dsum : 0.0;
+      }
+      __syncthreads();
+      const int p0 = __ldg(A.poly_off + ti), np = __ldg(A.poly_off + ti + 1) - p0;
+      for (int pt = tid; pt < np; pt += kBlock) {
+        const DevicePoly dp = A.poly[p0 + pt];
+        double v[kMaxPoly];
+        double prod = 1.0;
+#pragma unroll
+        for (int q = 0; q < kMaxPoly; ++q) {
+          v[q] = q < dp.order ? dnl[dp.k[q]] : 1.0;
+          prod *= v[q];
+        }
+        eacc += dp.w * prod;
+#pragma unroll
+        for (int q = 0; q < kMaxPoly; ++q) {
+          if (q < dp.order) {
+            double o = dp.w;
+#pragma unroll
+            for (int q2 = 0; q2 < kMaxPoly; ++q2)
+              if (q2 != q && q2 < dp.order) o *= v[q2];
+            atomicAdd(hnl + dp.k[q], o);
+          }
+        }
+      }
+    }
+    // ---------------------------------------------------------------- P4
+    for (int e = tid; e < T * Lh * kNPad; e += kBlock) sg[e] = Rc{R(0), R(0)};
+    __syncthreads();
+    // ---------------------------------------------------------------- P5
+    {
+      const int u0 = __ldg(A.unit_off + ti), nU = __ldg(A.unit_off + ti + 1) - u0;
+      while (true) {
+        int u = 0;
+        if (lane == 0) u = atomicAdd(misc + 10, 1);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= nU) break;
+        const DeviceUnit un = A.units[u0 + u];
+        double hv = 0.0;
+        if (act) {
+          hv = __ldg(A.w_lin + (size_t)un.itc * kNPad + n);
+          if (un.nl_slot >= 0) hv += hnl[un.nl_slot * kNPad + n];
+        }
+        R dsum = R(0);
+        dispatch_unit<true>(un, A.terms, sa, sg, Lh, n, half, act, (R)hv, dsum);
+        dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
+        if (half == 0 && act) eacc += __ldg(A.w_lin + (size_t)un.itc * kNPad + n) * (double)dsum;
+      }
+    }
+    __syncthreads();
+    // ---------------------------------------------------------------- P6
+    double fix = 0.0, fiy = 0.0, fiz = 0.0;
+    for (int jj = tid; jj < nkeep; jj += kBlock) {
+      const int k = nbk[jj];
+      const int j = __ldg(A.nbr_idx + k);
+      const double4 xj = A.x4[j];
+      const int tj = (int)xj.w;
+      double dx, dy, dz;
+      pair_disp(A, c, k, xi, xj, dx, dy, dz);
+      const double r = sqrt(dx * dx + dy * dy + dz * dz);
+      R f[kNPad], fd[kNPad];
+      radial(A.radial, F, (R)r, rc, f, fd, true);
+      const double ir = 1.0 / r;
+      ForceVis v{sg + (size_t)tj * Lh * kNPad, f, fd, F, (R)(dx * ir), (R)(dy * ir), (R)(dz * ir),
+                 R(0), R(0), R(0)};
+      sh_visit<LCAP, true>((R)dx, (R)dy, (R)dz, (R)r, L, v);
+      const double fx = v.fx, fy = v.fy, fz = v.fz;
+      fix += fx; fiy += fy; fiz += fz;
+      const int fj = A.fold ? __ldg(A.fold + j) : j;
+      atomicAdd(A.f + 3 * (size_t)fj, -fx);
+      atomicAdd(A.f + 3 * (size_t)fj + 1, -fy);
+      atomicAdd(A.f + 3 * (size_t)fj + 2, -fz);
+      // reference component order: xx yy zz yz zx xy
+      vir[0] -= dx * fx; vir[1] -= dy * fy; vir[2] -= dz * fz;
+      vir[3] -= dy * fz; vir[4] -= dz * fx; vir[5] -= dx * fy;
+    }
+    // block reduction of the centre's energy and force
+    double s0 = warp_sum(eacc), s1 = warp_sum(fix), s2 = warp_sum(fiy), s3 = warp_sum(fiz);
+    if (lane == 0) {
+      red[warp * 4 + 0] = s0; red[warp * 4 + 1] = s1;
+      red[warp * 4 + 2] = s2; red[warp * 4 + 3] = s3;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double e = 0, gx = 0, gy = 0, gz = 0;
+      for (int w = 0; w < kBlock / 32; ++w) {
+        e += red[w * 4]; gx += red[w * 4 + 1]; gy += red[w * 4 + 2]; gz += red[w * 4 + 3];
+      }
+      if (A.eatom) A.eatom[c] = e;
+      ecta += e;
+      const int fi = A.fold ? __ldg(A.fold + i) : i;
+      atomicAdd(A.f + 3 * (size_t)fi, gx);
+      atomicAdd(A.f + 3 * (size_t)fi + 1, gy);
+      atomicAdd(A.f + 3 * (size_t)fi + 2, gz);
+    }
+    __syncthreads();
+  }
+  // per-CTA partial sums: energy + virial (reference order)
+  double vals[7] = {ecta, vir[0], vir[1], vir[2], vir[3], vir[4], vir[5]};
+#pragma unroll
+  for (int q = 0; q < 7; ++q) vals[q] = warp_sum(vals[q]);
+  __syncthreads();
+  if (lane == 0)
+    for (int q = 0; q < 7; ++q) red[warp * 8 + q] = vals[q];
+  __syncthreads();
+  if (tid < 7) {
+    double s = 0;
+    for (int w = 0; w < kBlock / 32; ++w) s += red[w * 8 + tid];
+    A.partials[(size_t)blockIdx.x * 8 + tid] = s;
+  }
+}
+
+size_t smem_bytes(int T, int Lh, int nb_cap, int nl_cap) {
+  return smem_layout(T, Lh, nb_cap, nl_cap).total;
+}
+
+template <int LCAP>
+static cudaError_t prepare(size_t smem) {
+  return cudaFuncSetAttribute(fused_kernel<LCAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem);
+}
+
+template <int LCAP>
+static int occupancy(size_t smem) {
+  if (prepare<LCAP>(smem) != cudaSuccess) return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fused_kernel<LCAP>, kBlock, smem) !=
+      cudaSuccess)
+    return 0;
+  return nb;
+}
+
+int max_blocks(int L, size_t smem) {
+  if (L <= 6) return occupancy<6>(smem);
+  if (L <= 12) return occupancy<12>(smem);
+  return occupancy<20>(smem);
+}
+
+cudaError_t launch(int L, const KernelArgs& a, int grid, size_t smem, cudaStream_t s) {
+  cudaError_t e;
+  if (L <= 6) {
+    if ((e = prepare<6>(smem)) != cudaSuccess) return e;
+    fused_kernel<6><<<grid, kBlock, smem, s>>>(a);
+  } else if (L <= 12) {
+    if ((e = prepare<12>(smem)) != cudaSuccess) return e;
+    fused_kernel<12><<<grid, kBlock, smem, s>>>(a);
+  } else {
+    if ((e = prepare<20>(smem)) != cudaSuccess) return e;
+    fused_kernel<20><<<grid, kBlock, smem, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t init_constants() {
+  R A[kLhMax] = {}, B[kLhMax] = {}, LM[kLhMax] = {}, dg[kMaxL + 2] = {}, of[kMaxL + 2] = {},
+    ll[kMaxL + 1] = {};
+  for (int l = 2; l <= kMaxL; ++l) {
+    const double ls = l * l, lm1s = (l - 1) * (l - 1);
+    for (int m = 0; m <= l - 2; ++m) {
+      const double ms = m * m;
+      A[l * (l + 1) / 2 + m] = (R)std::sqrt((4.0 * ls - 1.0) / (ls - ms));
+      B[l * (l + 1) / 2 + m] = (R)(-std::sqrt((lm1s - ms) / (4.0 * lm1s - 1.0)));
+    }
+  }
+  for (int l = 0; l <= kMaxL; ++l)
+    for (int m = 0; m <= l; ++m) LM[l * (l + 1) / 2 + m] = (R)std::sqrt((double)(l - m) * (l + m + 1));
+  for (int m = 1; m <= kMaxL + 1; ++m) dg[m] = (R)(-std::sqrt(1.0 + 0.5 / m));
+  for (int m = 0; m <= kMaxL + 1; ++m) of[m] = (R)std::sqrt(2.0 * m + 3.0);
+  for (int l = 0; l <= kMaxL; ++l) ll[l] = (R)std::sqrt(0.5 * l * (l + 1));
+  cudaError_t e;
+  if ((e = cudaMemcpyToSymbol(cA, A, sizeof A)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(cB, B, sizeof B)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(cLM, LM, sizeof LM)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(cDiag, dg, sizeof dg)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(cOff, of, sizeof of)) != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(cLL, ll, sizeof ll);
+}
+
+}  // namespace MLIPG_TAG
+}  // namespace mlipg

@@ -1,0 +1,70 @@
+// Device-side interface of the fused MLIP kernel (see kernel_impl.cuh).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "model.hpp"
+
+namespace mlipg {
+
+constexpr int kBlock = 256;      // threads per CTA (8 warps)
+constexpr int kChunk = 32;       // neighbours staged per order-parameter chunk
+constexpr int kLhMax = (kMaxL + 1) * (kMaxL + 2) / 2;
+
+// Status bits raised by the kernel (read back by the host after each call).
+enum StatusBits : int {
+  kStatusNeighbourCapacity = 1,  // an atom had more neighbours inside rc than nb_cap
+  kStatusBadType = 2,            // an element index outside [0, T) in the inputs
+};
+
+struct KernelArgs {
+  // geometry (device pointers)
+  const double4* x4;      // [nall] position + element index (as double, <0 = skip)
+  const int* centers;     // [ncenters] atom indices whose energy/adjoint is evaluated
+  const int* nbr_off;     // [ncenters + 1] CSR into nbr_idx (indexed by centre position)
+  const int* nbr_idx;     // neighbour atom indices into x4
+  const int* img;         // optional per-pair packed image shift (null = none)
+  const double* cell;     // optional per-centre-cell lattice [ncell][9] (rows a1,a2,a3)
+  const int* center_cell; // optional cell id per centre (null = none)
+  const int* fold;        // optional atom -> force index (null = identity)
+  int ncenters;
+  // model (device pointers)
+  const DeviceTerm* terms;
+  const DeviceUnit* units;
+  const int* unit_off;    // [T + 1]
+  const DeviceUnit* nl_units;
+  const int* nl_off;      // [T + 1]
+  const DevicePoly* poly;
+  const int* poly_off;    // [T + 1]
+  const double* w_lin;    // [n_itc][16]
+  const double* radial;   // [F][2] (beta, mu)
+  int T, F, L, Lh, nb_cap, nl_cap;
+  double rc;
+  // outputs
+  double* f;              // [nforce][3], accumulated with atomics
+  double* eatom;          // [ncenters] (may be null)
+  double* partials;       // [gridDim.x][8]: energy, virial(6, reference order), spare
+  int* status;            // [1]
+};
+
+size_t fused_smem_bytes(bool fp64, int T, int Lh, int nb_cap, int nl_cap);
+int fused_max_blocks_per_sm(bool fp64, int L, size_t smem);
+cudaError_t launch_fused(bool fp64, int L, const KernelArgs& a, int grid, size_t smem,
+                         cudaStream_t s);
+cudaError_t launch_finalize(const double* partials, int nparts, double* out8, cudaStream_t s);
+cudaError_t init_device_constants();
+
+}  // namespace mlipg
+
+namespace mlipg {
+#define MLIPG_DECL_PREC(tag)                                                           \
+  namespace tag {                                                                      \
+  size_t smem_bytes(int T, int Lh, int nb_cap, int nl_cap);                            \
+  int max_blocks(int L, size_t smem);                                                  \
+  cudaError_t launch(int L, const KernelArgs& a, int grid, size_t smem, cudaStream_t s); \
+  cudaError_t init_constants();                                                        \
+  }
+MLIPG_DECL_PREC(f64)
+MLIPG_DECL_PREC(f32)
+#undef MLIPG_DECL_PREC
+}  // namespace mlipg

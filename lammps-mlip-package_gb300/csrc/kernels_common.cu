@@ -1,0 +1,50 @@
+// Precision dispatch and the deterministic partial-sum reduction.
+#include "kernels.cuh"
+
+namespace mlipg {
+
+static_assert(sizeof(DeviceTerm) == 16, "DeviceTerm must be 16 bytes");
+static_assert(sizeof(DeviceUnit) == 32, "DeviceUnit must be 32 bytes");
+static_assert(sizeof(DevicePoly) == 32, "DevicePoly must be 32 bytes");
+
+size_t fused_smem_bytes(bool fp64, int T, int Lh, int nb_cap, int nl_cap) {
+  return fp64 ? f64::smem_bytes(T, Lh, nb_cap, nl_cap) : f32::smem_bytes(T, Lh, nb_cap, nl_cap);
+}
+
+int fused_max_blocks_per_sm(bool fp64, int L, size_t smem) {
+  return fp64 ? f64::max_blocks(L, smem) : f32::max_blocks(L, smem);
+}
+
+cudaError_t launch_fused(bool fp64, int L, const KernelArgs& a, int grid, size_t smem,
+                         cudaStream_t s) {
+  return fp64 ? f64::launch(L, a, grid, smem, s) : f32::launch(L, a, grid, smem, s);
+}
+
+cudaError_t init_device_constants() {
+  cudaError_t e = f64::init_constants();
+  if (e != cudaSuccess) return e;
+  return f32::init_constants();
+}
+
+// Sums the per-CTA partials [nparts][8] in a fixed order (deterministic).
+__global__ void finalize_kernel(const double* __restrict__ parts, int nparts, double* out) {
+  __shared__ double red[8][33];
+  const int q = threadIdx.y;        // 0..7
+  const int lane = threadIdx.x;     // 0..31
+  double s = 0.0;
+  for (int p = lane; p < nparts; p += 32) s += parts[(size_t)p * 8 + q];
+  red[q][lane] = s;
+  __syncthreads();
+  if (lane == 0) {
+    double t = 0.0;
+    for (int k = 0; k < 32; ++k) t += red[q][k];
+    out[q] = t;
+  }
+}
+
+cudaError_t launch_finalize(const double* partials, int nparts, double* out8, cudaStream_t s) {
+  finalize_kernel<<<1, dim3(32, 8), 0, s>>>(partials, nparts, out8);
+  return cudaGetLastError();
+}
+
+}  // namespace mlipg

@@ -1,0 +1,615 @@
+// Host-side model: parser, coupling table, enumeration and device schedules.
+// See model.hpp for the reference functions restated here.
+#include "model.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <map>
+#include <queue>
+#include <set>
+#include <sstream>
+
+namespace mlipg {
+
+namespace {
+
+#include "gtinv_table.inc"  // defines kGtinvTableText (generated from data/gtinv_table.txt)
+
+struct Table {
+  std::vector<std::vector<int>> l;
+  std::vector<std::vector<std::vector<int>>> m;
+  std::vector<std::vector<double>> c;
+};
+
+const Table& table() {
+  static Table t = [] {
+    Table tab;
+    std::stringstream all;
+    std::stringstream src(kGtinvTableText);
+    std::string line;
+    while (std::getline(src, line)) {
+      if (!line.empty() && line[0] == '#') continue;
+      all << line << '\n';
+    }
+    int n = 0;
+    all >> n;
+    tab.l.resize(n);
+    tab.m.resize(n);
+    tab.c.resize(n);
+    for (int i = 0; i < n; ++i) {
+      int q = 0;
+      all >> q;
+      tab.l[i].resize(q);
+      for (int k = 0; k < q; ++k) all >> tab.l[i][k];
+      int nt = 0;
+      all >> nt;
+      tab.m[i].assign(nt, std::vector<int>(q));
+      tab.c[i].assign(nt, 0.0);
+      for (int j = 0; j < nt; ++j) {
+        all >> tab.c[i][j];
+        for (int k = 0; k < q; ++k) all >> tab.m[i][j][k];
+      }
+    }
+    return tab;
+  }();
+  return t;
+}
+
+bool getline_ss(std::ifstream& in, std::stringstream& ss, std::string& err) {
+  std::string l;
+  if (!std::getline(in, l)) {
+    err = "potential file is truncated";
+    return false;
+  }
+  ss.str(l);
+  ss.clear();
+  return true;
+}
+
+std::vector<std::pair<int, int>> type_pairs_mapping(int T) {
+  std::vector<std::pair<int, int>> v;
+  for (int a = 0; a < T; ++a)
+    for (int b = a; b < T; ++b) v.push_back({a, b});
+  return v;
+}
+
+std::vector<char> intersection_of(int T, const std::vector<std::pair<int, int>>& tpm,
+                                  const std::vector<int>& comb) {
+  std::vector<char> in(T, 1);
+  for (int idx : comb)
+    for (int t = 0; t < T; ++t)
+      if (t != tpm[idx].first && t != tpm[idx].second) in[t] = 0;
+  return in;
+}
+
+bool any_of(const std::vector<char>& v) {
+  return std::any_of(v.begin(), v.end(), [](char e) { return e != 0; });
+}
+
+// Multisets of size r over {0..n-1} in lexicographic order (the breadth-first
+// generation of mlipkk_utils.cpp:33-58 visits them in this order).
+void multisets_lex(int n, int r, std::vector<std::vector<int>>& out) {
+  std::vector<int> c(r, 0);
+  if (r == 0) return;
+  while (true) {
+    out.push_back(c);
+    int k = r - 1;
+    while (k >= 0 && c[k] == n - 1) --k;
+    if (k < 0) break;
+    int v = c[k] + 1;
+    for (int j = k; j < r; ++j) c[j] = v;
+  }
+}
+
+// Non-increasing sequences of length r with first element ascending, then
+// lexicographic: the "historical" order of mlipkk_utils.cpp:64-98.
+void sequences_gtinv(int n, int r, std::vector<std::vector<int>>& out) {
+  std::vector<int> c(r, 0);
+  for (int first = 0; first < n; ++first) {
+    c[0] = first;
+    for (int j = 1; j < r; ++j) c[j] = 0;
+    while (true) {
+      out.push_back(c);
+      int k = r - 1;
+      while (k >= 1 && c[k] == c[k - 1]) --k;
+      if (k < 1) break;
+      ++c[k];
+      for (int j = k + 1; j < r; ++j) c[j] = 0;
+    }
+  }
+}
+
+void screen(const Potential& p, Model& M) {
+  const Table& tab = table();
+  int count = 0;
+  for (size_t i = 0; i < tab.l.size(); ++i) {
+    const auto& lc = tab.l[i];
+    const int order = (int)lc.size();
+    bool req = true;
+    if (order > 1) {
+      if (order > p.gtinv_order || lc.back() > p.gtinv_maxl[order - 2]) req = false;
+      else if (p.gtinv_sym[order - 2] &&
+               (int)std::count(lc.begin(), lc.end(), lc[0]) != order)
+        req = false;
+    }
+    if (!req) continue;
+    M.irr_l.push_back(lc);
+    M.irr_first.push_back(count);
+    M.irr_nterms.push_back((int)tab.m[i].size());
+    for (size_t j = 0; j < tab.m[i].size(); ++j) {
+      std::vector<int> lm(order);
+      for (int k = 0; k < order; ++k) lm[k] = lc[k] * lc[k] + lc[k] + tab.m[i][j][k];
+      M.term_lm.push_back(lm);
+      M.term_c.push_back(tab.c[i][j]);
+      ++count;
+    }
+  }
+}
+
+void build_itc(Model& M) {
+  const int T = M.T, ntc = T * (T + 1) / 2;
+  auto tpm = type_pairs_mapping(T);
+  const int max_order = (int)M.irr_l.back().size();
+  std::vector<std::vector<std::vector<int>>> uniq(max_order);
+  for (int order = 1; order <= max_order; ++order) {
+    std::vector<std::vector<int>> all;
+    multisets_lex(ntc, order, all);
+    for (auto& c : all)
+      if (any_of(intersection_of(T, tpm, c))) uniq[order - 1].push_back(c);
+  }
+  for (int i = 0; i < (int)M.irr_l.size(); ++i) {
+    const auto& lc = M.irr_l[i];
+    const int order = (int)lc.size();
+    std::set<std::vector<std::pair<int, int>>> sets;
+    for (auto tcomb : uniq[order - 1]) {
+      do {
+        std::vector<std::pair<int, int>> ms(order);
+        for (int j = 0; j < order; ++j) ms[j] = {lc[j], tcomb[j]};
+        std::sort(ms.begin(), ms.end());
+        sets.insert(ms);
+      } while (std::next_permutation(tcomb.begin(), tcomb.end()));
+    }
+    for (auto& ms : sets) {
+      ITC x;
+      x.irreps = i;
+      for (auto& pr : ms) x.type_combs.push_back(pr.second);
+      x.inter = intersection_of(T, tpm, x.type_combs);
+      M.itc.push_back(x);
+    }
+  }
+}
+
+std::vector<char> poly_intersection(const Model& M, const std::vector<int>& fc) {
+  std::vector<char> in(M.T, 1);
+  for (int f : fc) {
+    const auto& x = M.itc[f % M.n_itc].inter;
+    for (int t = 0; t < M.T; ++t) in[t] = in[t] && x[t];
+  }
+  return in;
+}
+
+bool build_poly(Model& M, std::string& err) {
+  const int D = M.D, mt = M.pot.model_type, maxp = M.pot.maxp;
+  const size_t limit = 200000000;  // entries; larger models are not representable
+  auto check = [&](size_t n) {
+    if (n > limit) {
+      err = "polynomial index too large for this model_type";
+      return false;
+    }
+    return true;
+  };
+  if (mt == 1) {
+    for (int po = 1; po <= maxp; ++po)
+      for (int f = 0; f < D; ++f)
+        if (any_of(M.itc[f % M.n_itc].inter)) M.poly.push_back(std::vector<int>(po, f));
+  } else if (mt == 2) {
+    for (int po = 1; po <= maxp; ++po) {
+      double est = 1;
+      for (int k = 0; k < po; ++k) est = est * (D + k) / (k + 1);
+      if (!check((size_t)est * po)) return false;
+      std::vector<std::vector<int>> all;
+      sequences_gtinv(D, po, all);
+      for (auto& fc : all)
+        if (any_of(poly_intersection(M, fc))) M.poly.push_back(fc);
+    }
+  } else if (mt == 3 || mt == 4) {
+    std::vector<int> lower;
+    for (int f = 0; f < D; ++f) {
+      const int q = (int)M.itc[f % M.n_itc].type_combs.size();
+      if ((mt == 3 && q == 1) || (mt == 4 && q <= 2)) lower.push_back(f);
+    }
+    for (int f = 0; f < D; ++f) M.poly.push_back({f});
+    for (int po = 2; po <= maxp; ++po) {
+      std::vector<std::vector<int>> all;
+      sequences_gtinv((int)lower.size(), po, all);
+      for (auto& ch : all) {
+        std::vector<int> fc(po);
+        for (int k = 0; k < po; ++k) fc[k] = lower[ch[k]];
+        if (any_of(poly_intersection(M, fc))) M.poly.push_back(fc);
+      }
+    }
+  } else {
+    err = "Unknown model_type: " + std::to_string(mt);
+    return false;
+  }
+  return true;
+}
+
+// Folds each conjugate pair of raw terms into one canonical DeviceTerm.
+bool fold_terms(Model& M, std::string& err) {
+  for (size_t k = 0; k < M.irr_l.size(); ++k) {
+    const auto& lc = M.irr_l[k];
+    const int q = (int)lc.size();
+    M.irr_cfirst.push_back((int)M.cterms.size());
+    std::map<std::vector<int>, double> byM;
+    for (int j = 0; j < M.irr_nterms[k]; ++j) {
+      const int t = M.irr_first[k] + j;
+      std::vector<int> mv(q);
+      for (int p = 0; p < q; ++p) mv[p] = M.term_lm[t][p] - lc[p] * lc[p] - lc[p];
+      byM[mv] = M.term_c[t];
+    }
+    int n = 0;
+    for (int j = 0; j < M.irr_nterms[k]; ++j) {
+      const int t = M.irr_first[k] + j;
+      std::vector<int> mv(q), neg(q);
+      for (int p = 0; p < q; ++p) {
+        mv[p] = M.term_lm[t][p] - lc[p] * lc[p] - lc[p];
+        neg[p] = -mv[p];
+      }
+      int first_nz = 0;
+      for (int p = 0; p < q; ++p)
+        if (mv[p] != 0) { first_nz = mv[p]; break; }
+      const bool self = (first_nz == 0);
+      if (first_nz > 0) {
+        if (!byM.count(neg)) {
+          err = "coupling table is not closed under m -> -m";
+          return false;
+        }
+        continue;  // represented by its partner
+      }
+      if (!self && !byM.count(neg)) {
+        err = "coupling table is not closed under m -> -m";
+        return false;
+      }
+      DeviceTerm d{};
+      double c = M.term_c[t];
+      uint16_t code = 0;
+      for (int p = 0; p < q; ++p) {
+        const int l = lc[p], m = mv[p];
+        d.lmh[p] = (uint8_t)(l * (l + 1) / 2 + l - std::abs(m));
+        int sc;
+        if (m > 0) {
+          if (m % 2) c = -c;
+          sc = kSlotConj;
+        } else if (m < 0) {
+          sc = kSlotNormal;
+        } else {
+          sc = self ? kSlotSelf : kSlotMZero;
+        }
+        code |= (uint16_t)(sc << (2 * p));
+      }
+      if (self) code |= (uint16_t)(1u << 12);
+      d.c = c;
+      d.code = code;
+      M.cterms.push_back(d);
+      ++n;
+    }
+    M.irr_cnterms.push_back(n);
+  }
+  return true;
+}
+
+void build_schedules(Model& M) {
+  const int T = M.T, F = M.F;
+  // nonlinear itc: appear in any polynomial term of order >= 2
+  std::vector<char> is_nl(M.n_itc, 0);
+  for (auto& row : M.poly)
+    if (row.size() >= 2)
+      for (int f : row) is_nl[f % M.n_itc] = 1;
+  M.w_lin.assign((size_t)M.n_itc * kNPad, 0.0);
+  for (size_t pi = 0; pi < M.poly.size(); ++pi)
+    if (M.poly[pi].size() == 1) {
+      const int f = M.poly[pi][0];
+      M.w_lin[(size_t)(f % M.n_itc) * kNPad + f / M.n_itc] += M.pot.coeffs[pi];
+    }
+  M.sched.assign(T, Schedule());
+  M.max_nl = 0;
+  for (int t = 0; t < T; ++t) {
+    Schedule& S = M.sched[t];
+    std::vector<int> slot(M.n_itc, -1);
+    for (int i = 0; i < M.n_itc; ++i) {
+      if (!M.itc[i].inter[t]) continue;
+      const int k = M.itc[i].irreps;
+      DeviceUnit u{};
+      u.itc = i;
+      u.term0 = M.irr_cfirst[k];
+      u.nterm = M.irr_cnterms[k];
+      u.q = (uint8_t)M.irr_l[k].size();
+      for (int p = 0; p < u.q; ++p) u.s[p] = (uint8_t)M.other_type[M.itc[i].type_combs[p] * T + t];
+      u.nl_slot = -1;
+      if (is_nl[i]) {
+        u.nl_slot = (int)S.nl_units.size();
+        slot[i] = u.nl_slot;
+        S.nl_units.push_back(u);
+      }
+      S.units.push_back(u);
+    }
+    // longest units first, grouped by order
+    std::stable_sort(S.units.begin(), S.units.end(), [](const DeviceUnit& a, const DeviceUnit& b) {
+      if (a.q != b.q) return a.q > b.q;
+      return a.nterm > b.nterm;
+    });
+    M.max_nl = std::max(M.max_nl, (int)S.nl_units.size());
+    for (size_t pi = 0; pi < M.poly.size(); ++pi) {
+      const auto& row = M.poly[pi];
+      if (row.size() < 2) continue;
+      bool ok = true;
+      for (int f : row) ok = ok && M.itc[f % M.n_itc].inter[t];
+      if (!ok) continue;
+      DevicePoly dp{};
+      dp.w = M.pot.coeffs[pi];
+      dp.order = (int)row.size();
+      for (int p = 0; p < dp.order; ++p)
+        dp.k[p] = slot[row[p] % M.n_itc] * kNPad + row[p] / M.n_itc;
+      S.poly.push_back(dp);
+    }
+    (void)F;
+  }
+}
+
+}  // namespace
+
+bool read_potential(const std::string& path, Potential& p, std::string& err) {
+  std::ifstream in(path);
+  if (!in) {
+    err = "Could not open mlip file: " + path;
+    return false;
+  }
+  std::string line;
+  if (!std::getline(in, line)) {
+    err = "potential file is empty";
+    return false;
+  }
+  {
+    // line 1: element names, then a "# element" comment
+    std::stringstream ss(line);
+    std::string tok;
+    while (ss >> tok) {
+      if (tok[0] == '#') break;
+      p.elements.push_back(tok);
+    }
+  }
+  if (p.elements.empty()) {
+    err = "no element names on the first line of the potential file";
+    return false;
+  }
+  std::stringstream ss;
+  std::string s;
+  if (!getline_ss(in, ss, err)) return false;
+  ss >> p.cutoff;
+  if (!getline_ss(in, ss, err)) return false;
+  ss >> s;
+  if (s != "gaussian") {
+    err = "Unknown pair_type: " + s;
+    return false;
+  }
+  if (!getline_ss(in, ss, err)) return false;
+  ss >> s;
+  if (s == "pair") {
+    err = "NotImplemented: des_type == pair";
+    return false;
+  }
+  if (s != "gtinv") {
+    err = "Unknown des_type: " + s;
+    return false;
+  }
+  if (!getline_ss(in, ss, err)) return false;
+  ss >> p.model_type;
+  if (!getline_ss(in, ss, err)) return false;
+  ss >> p.maxp;
+  if (!getline_ss(in, ss, err)) return false;
+  ss >> p.maxl;
+  if (!getline_ss(in, ss, err)) return false;
+  ss >> p.gtinv_order;
+  const int nm = p.gtinv_order - 1;
+  if (nm < 0 || nm > kMaxOrder - 1) {
+    err = "gtinv_order out of range";
+    return false;
+  }
+  if (!getline_ss(in, ss, err)) return false;
+  p.gtinv_maxl.assign(nm, 0);
+  for (auto& v : p.gtinv_maxl) ss >> v;
+  if (!getline_ss(in, ss, err)) return false;
+  p.gtinv_sym.assign(nm, 0);
+  for (auto& v : p.gtinv_sym) ss >> v;
+  long nc = 0;
+  if (!getline_ss(in, ss, err)) return false;
+  ss >> nc;
+  if (nc < 0) {
+    err = "negative number of regression coefficients";
+    return false;
+  }
+  p.coeffs.assign(nc, 0.0);
+  if (!getline_ss(in, ss, err)) return false;
+  for (auto& v : p.coeffs) ss >> v;
+  if (!ss && nc > 0) {
+    err = "too few regression coefficients";
+    return false;
+  }
+  if (!getline_ss(in, ss, err)) return false;
+  for (long k = 0; k < nc; ++k) {
+    double sc = 1.0;
+    ss >> sc;
+    p.coeffs[k] /= sc;
+  }
+  int npar = 0;
+  if (!getline_ss(in, ss, err)) return false;
+  ss >> npar;
+  for (int k = 0; k < npar; ++k) {
+    if (!getline_ss(in, ss, err)) return false;
+    double b = 0, m = 0;
+    ss >> b >> m;
+    p.params.push_back({b, m});
+  }
+  if (!getline_ss(in, ss, err)) return false;
+  p.masses.assign(p.elements.size(), 0.0);
+  for (auto& m : p.masses) ss >> m;
+  return true;
+}
+
+bool build_model(Model& M, std::string& err) {
+  const Potential& p = M.pot;
+  M.T = (int)p.elements.size();
+  if (M.T > kMaxTypes) {
+    err = "more than 8 elements are not supported";
+    return false;
+  }
+  M.TC = M.T * (M.T + 1) / 2;
+  M.F = (int)p.params.size();
+  M.L = p.maxl;
+  if (M.F < 1 || M.F > kNPad) {
+    err = "number of radial functions must be in [1, 16]";
+    return false;
+  }
+  if (M.L < 0 || M.L > kMaxL) {
+    err = "max_l must be in [0, 20]";
+    return false;
+  }
+  if (p.cutoff <= 0) {
+    err = "cutoff must be positive";
+    return false;
+  }
+  M.Lh = (M.L + 1) * (M.L + 2) / 2;
+  screen(p, M);
+  // every screened term must reference l <= max_l
+  for (auto& lc : M.irr_l)
+    if (lc.back() > M.L) {
+      err = "gtinv_maxl exceeds max_l";
+      return false;
+    }
+  build_itc(M);
+  M.n_itc = (int)M.itc.size();
+  M.D = M.F * M.n_itc;
+  if (!build_poly(M, err)) return false;
+  if (M.poly.size() != p.coeffs.size()) {
+    char b[200];
+    snprintf(b, sizeof b, "number of regression coefficients %zu does not match the model (%zu)",
+             p.coeffs.size(), M.poly.size());
+    err = b;
+    return false;
+  }
+  for (auto& row : M.poly)
+    if ((int)row.size() > kMaxPoly) {
+      err = "polynomial order above 4 is not supported";
+      return false;
+    }
+  M.type_pairs.assign(M.T * M.T, 0);
+  int cnt = 0;
+  for (int a = 0; a < M.T; ++a)
+    for (int b = a; b < M.T; ++b) M.type_pairs[a * M.T + b] = M.type_pairs[b * M.T + a] = cnt++;
+  M.other_type.assign(M.TC * M.T, -1);
+  auto tpm = type_pairs_mapping(M.T);
+  for (int tc = 0; tc < M.TC; ++tc) {
+    M.other_type[tc * M.T + tpm[tc].first] = tpm[tc].second;
+    M.other_type[tc * M.T + tpm[tc].second] = tpm[tc].first;
+  }
+  if (!fold_terms(M, err)) return false;
+  build_schedules(M);
+  return true;
+}
+
+bool count_coefficients(int n_types, int model_type, int maxp, int maxl, int gtinv_order,
+                        const int* gtinv_maxl, const int* gtinv_sym, int n_fn,
+                        long long* n_coeffs, long long* n_features, std::string& err) {
+  Model M;
+  M.pot.elements.assign(n_types, "X");
+  M.pot.model_type = model_type;
+  M.pot.maxp = maxp;
+  M.pot.maxl = maxl;
+  M.pot.gtinv_order = gtinv_order;
+  M.pot.gtinv_maxl.assign(gtinv_maxl, gtinv_maxl + gtinv_order - 1);
+  M.pot.gtinv_sym.assign(gtinv_sym, gtinv_sym + gtinv_order - 1);
+  M.T = n_types;
+  M.F = n_fn;
+  if (n_types < 1 || n_types > kMaxTypes || gtinv_order < 1 || gtinv_order > kMaxOrder) {
+    err = "invalid model specification";
+    return false;
+  }
+  screen(M.pot, M);
+  build_itc(M);
+  M.n_itc = (int)M.itc.size();
+  const long long D = (long long)n_fn * M.n_itc;
+  *n_features = D;
+  // polynomial count by inclusion-exclusion over element subsets: number of
+  // multisets of size p whose features share at least one element
+  auto mask_of = [&](long long f) {
+    int m = 0;
+    for (int t = 0; t < n_types; ++t)
+      if (M.itc[f % M.n_itc].inter[t]) m |= 1 << t;
+    return m;
+  };
+  auto multichoose = [](long long n, int p) {
+    long double v = 1;
+    for (int k = 0; k < p; ++k) v = v * (n + k) / (k + 1);
+    return (long long)(v + 0.5);
+  };
+  auto count_from = [&](const std::vector<long long>& feats, int p) {
+    std::vector<long long> by_mask(1 << n_types, 0);
+    for (long long f : feats) by_mask[mask_of(f)]++;
+    long long tot = 0;
+    for (int S = 1; S < (1 << n_types); ++S) {
+      long long nS = 0;
+      for (int m = 0; m < (1 << n_types); ++m)
+        if ((m & S) == S) nS += by_mask[m];
+      const int bits = __builtin_popcount(S);
+      tot += ((bits % 2) ? 1 : -1) * multichoose(nS, p);
+    }
+    return tot;
+  };
+  std::vector<long long> all, lower;
+  for (long long f = 0; f < D; ++f) {
+    all.push_back(f);
+    const int q = (int)M.itc[f % M.n_itc].type_combs.size();
+    if ((model_type == 3 && q == 1) || (model_type == 4 && q <= 2)) lower.push_back(f);
+  }
+  long long n = 0;
+  if (model_type == 1) {
+    long long valid = 0;
+    for (long long f : all) valid += mask_of(f) != 0;
+    n = valid * maxp;
+  } else if (model_type == 2) {
+    for (int p = 1; p <= maxp; ++p) n += count_from(all, p);
+  } else if (model_type == 3 || model_type == 4) {
+    n = D;
+    for (int p = 2; p <= maxp; ++p) n += count_from(lower, p);
+  } else {
+    err = "Unknown model_type";
+    return false;
+  }
+  *n_coeffs = n;
+  return true;
+}
+
+double flops_per_atom_step(const Model& M, int t, double nbar) {
+  double f = nbar * M.F * M.Lh * (4.0 + 30.0);
+  for (int i = 0; i < M.n_itc; ++i) {
+    if (!M.itc[i].inter[t]) continue;
+    const int k = M.itc[i].irreps;
+    const double Ti = M.irr_nterms[k];
+    const int q = (int)M.irr_l[k].size();
+    f += M.F * Ti * (6.0 * (q - 1) + 3.0);
+    f += M.F * Ti * q * (6.0 * std::max(q - 2, 0) + 4.0);
+  }
+  for (size_t pi = 0; pi < M.poly.size(); ++pi) {
+    bool ok = true;
+    for (int ff : M.poly[pi]) ok = ok && M.itc[ff % M.n_itc].inter[t];
+    if (!ok) continue;
+    const double p = (double)M.poly[pi].size();
+    f += 2.0 * p + 2.0 * p * (p - 1.0);
+  }
+  return f;
+}
+
+}  // namespace mlipg

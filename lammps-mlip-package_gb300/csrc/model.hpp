@@ -1,0 +1,119 @@
+// Host-side model for the GB300 MLIP (gtinv) path: potential-file parser,
+// coupling table, model structure and the per-element work schedules that
+// the device kernel consumes.
+//
+// Reference interfaces restated here (same meaning, same ordering):
+//   potential file        src/USER-MLIP/mlipkk_potential_parser.cpp:14-105
+//   table screening       src/USER-MLIP/mlipkk_gtinv_data_reader.cpp:18-76
+//   irreps x typecomb     src/USER-MLIP/mlipkk_irreps_type.cpp:48-100
+//   polynomial index      src/USER-MLIP/mlipkk_polynomial.cpp:12-208
+//   feature index         fidx = n * n_itc + itc (mlipkk_polynomial.cpp:48-51)
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace mlipg {
+
+constexpr int kNPad = 16;      // radial index n is padded to 16 lanes
+constexpr int kMaxOrder = 6;   // coupling table orders 1..6
+constexpr int kMaxPoly = 4;    // polynomial terms of order <= 4
+constexpr int kMaxL = 20;      // coupling table angular momenta <= 20
+constexpr int kMaxTypes = 8;
+
+struct Potential {
+  std::vector<std::string> elements;
+  std::vector<double> masses;
+  double cutoff = 0;
+  int model_type = 0, maxp = 0, maxl = 0, gtinv_order = 0;
+  std::vector<int> gtinv_maxl, gtinv_sym;
+  std::vector<double> coeffs;                       // divided by the scales
+  std::vector<std::pair<double, double>> params;    // (beta, mu) per radial function
+};
+
+// Canonical member of a conjugate pair of coupling terms, sign-folded.
+// The table is closed under m -> -m with equal coefficients, and
+// a_{l,-m} = (-1)^m conj(a_{l,m}); so the pair (m, -m) contributes
+// 2 Re(c' prod a~) to the invariant, where a~ are the stored m <= 0 order
+// parameters (conjugated for slots with m > 0) and c' carries the signs.
+// Self-conjugate terms (all m = 0) contribute c' prod a~ once.
+struct DeviceTerm {       // 16 bytes, read warp-uniformly
+  double c;               // folded coefficient c'
+  uint8_t lmh[kMaxOrder]; // LMInfoIdx l(l+1)/2 + l - |m| of each slot
+  uint16_t code;          // 2 bits per slot (see SlotCode) + bit 12 = self-conjugate
+};
+enum SlotCode : int { kSlotNormal = 0, kSlotConj = 1, kSlotMZero = 2, kSlotSelf = 3 };
+
+// One (irreps, element tuple) for a given centre element: the invariant
+// d(n) = sum over its canonical terms, for all n at once (16 lanes).
+struct DeviceUnit {       // 32 bytes
+  int itc;                // irreps-typecomb index (feature fidx = n*ITC + itc)
+  int term0;              // first canonical term
+  int nterm;              // number of canonical terms
+  int nl_slot;            // slot of this itc among nonlinear features, -1 if linear only
+  uint8_t s[kMaxOrder];   // neighbour element of each slot
+  uint8_t q;              // order
+  uint8_t pad;
+  int pad2[2];
+};
+
+// Polynomial term of order >= 2 valid for a centre element.
+struct DevicePoly {       // 32 bytes
+  double w;
+  int k[kMaxPoly];        // index into the nonlinear-feature array: slot*16 + n
+  int order;
+  int pad;
+};
+
+struct ITC {
+  int irreps;
+  std::vector<int> type_combs;
+  std::vector<char> inter;
+};
+
+struct Schedule {         // per centre element
+  std::vector<DeviceUnit> units;     // all valid itc, sorted by cost
+  std::vector<DeviceUnit> nl_units;  // nonlinear itc, nl_slot = position
+  std::vector<DevicePoly> poly;      // order >= 2 polynomial terms
+};
+
+struct Model {
+  Potential pot;
+  int T = 0, TC = 0, F = 0, L = 0, Lh = 0;
+  // screened irreps
+  std::vector<std::vector<int>> irr_l;
+  std::vector<int> irr_first, irr_nterms;     // raw (unfolded) terms
+  std::vector<std::vector<int>> term_lm;      // raw term -> LMIdx per slot
+  std::vector<double> term_c;
+  std::vector<int> irr_cfirst, irr_cnterms;   // canonical folded terms
+  std::vector<DeviceTerm> cterms;
+  std::vector<ITC> itc;
+  int n_itc = 0, D = 0;
+  std::vector<std::vector<int>> poly;         // PolynomialIdx -> FeatureIdx list
+  std::vector<double> w_lin;                  // [n_itc][kNPad], order-1 weights
+  std::vector<int> type_pairs;                // [T*T] -> tc
+  std::vector<int> other_type;                // [TC*T]
+  std::vector<Schedule> sched;                // [T]
+  int max_nl = 0;                             // max nonlinear itc over elements
+};
+
+// Parses a potential file; returns false with `err` set on failure.
+bool read_potential(const std::string& path, Potential& p, std::string& err);
+
+// Builds the complete model (table screening, enumeration, schedules).
+bool build_model(Model& m, std::string& err);
+
+// Counts coefficients and features for a model specification.
+bool count_coefficients(int n_types, int model_type, int maxp, int maxl, int gtinv_order,
+                        const int* gtinv_maxl, const int* gtinv_sym, int n_fn,
+                        long long* n_coeffs, long long* n_features, std::string& err);
+
+// Algorithmic flop count per atom step for a centre element with nbar
+// neighbours inside the cutoff (counting rule: complex*complex 6,
+// real*complex 2, complex add 2, real fma 2; transcendentals and
+// recomputation excluded).
+double flops_per_atom_step(const Model& m, int elem, double nbar);
+
+}  // namespace mlipg

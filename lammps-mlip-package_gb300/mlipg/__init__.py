@@ -1,0 +1,196 @@
+"""Python binding (ctypes) of libmlipg.so, the GB300 MLIP C ABI (include/mlipg.h).
+
+This mirrors how LAMMPS drives the reference pair style: create a handle
+from a potential file (``pair_coeff`` reads it), map LAMMPS types to file
+elements, then call `Potential.compute` with owned+ghost coordinates and a
+full neighbour list.  There is no CPU fallback: on a machine without a GPU
+the model can be inspected but every compute raises `MlipgError` with
+``MLIPG_ENOGPU``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+ERRORS = {1: "EINVAL", 2: "EIO", 3: "ENOMEM", 4: "ECUDA", 5: "ENOTSUP", 6: "ECAPACITY",
+          7: "ENOGPU", 8: "ETIMEDOUT", 9: "EBUSY"}
+
+_lib = None
+
+
+class MlipgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+def lib():
+    """Loads libmlipg.so (building it in-tree first if it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build()
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    i32 = ctypes.c_int
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    llp = ctypes.POINTER(ctypes.c_longlong)
+    sig = {
+        "mlipg_last_error": (ctypes.c_char_p, [P]),
+        "mlipg_create": (i32, [ctypes.c_char_p, i32, ctypes.POINTER(P)]),
+        "mlipg_destroy": (i32, [P]),
+        "mlipg_set_precision": (i32, [P, i32]),
+        "mlipg_num_elements": (i32, [P]),
+        "mlipg_element_name": (ctypes.c_char_p, [P, i32]),
+        "mlipg_element_mass": (ctypes.c_double, [P, i32]),
+        "mlipg_cutoff": (ctypes.c_double, [P]),
+        "mlipg_set_type_map": (i32, [P, i32, ctypes.POINTER(ctypes.c_char_p)]),
+        "mlipg_compute": (i32, [P, i32, i32, dp, ip, i32, ip, ip, ctypes.POINTER(ip), i32, i32,
+                                dp, dp, dp, dp]),
+        "mlipg_compute_device": (i32, [P, i32, P, P, P, P, P, P, P, P, i32, P, P, P]),
+        "mlipg_stream": (P, [P]),
+        "mlipg_device_status": (i32, [P, ip]),
+        "mlipg_count_coefficients": (i32, [i32, i32, i32, i32, i32, ip, ip, i32, llp, llp]),
+        "mlipg_model_info": (i32, [P, llp]),
+        "mlipg_dump_itc": (ctypes.c_long, [P, ip, ctypes.c_long]),
+        "mlipg_dump_poly": (ctypes.c_long, [P, ip, ctypes.c_long]),
+        "mlipg_flops_per_atom_step": (ctypes.c_double, [P, i32, ctypes.c_double]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc, h=None):
+    if rc != 0:
+        msg = lib().mlipg_last_error(h)
+        raise MlipgError(rc, msg.decode() if msg else "")
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def count_coefficients(n_types, model_type, maxp, maxl, gtinv_order, gtinv_maxl, gtinv_sym,
+                       n_fn):
+    """(n_coeffs, n_features) of a model specification (no GPU needed)."""
+    ml = np.ascontiguousarray(list(gtinv_maxl) or [0], dtype=np.int32)
+    sy = np.ascontiguousarray([int(s) for s in gtinv_sym] or [0], dtype=np.int32)
+    nc = ctypes.c_longlong()
+    nf = ctypes.c_longlong()
+    _check(lib().mlipg_count_coefficients(n_types, model_type, maxp, maxl, gtinv_order, _ip(ml),
+                                          _ip(sy), n_fn, ctypes.byref(nc), ctypes.byref(nf)))
+    return nc.value, nf.value
+
+
+class Potential:
+    """A loaded potential on the current CUDA device (one handle, one stream)."""
+
+    INFO = ["T", "F", "L", "Lh", "n_irreps", "n_terms", "n_folded_terms", "ITC", "D",
+            "n_coeffs", "model_type", "maxp", "max_nonlinear_itc"]
+
+    def __init__(self, path: str, precision: int = PREC_FP64):
+        h = ctypes.c_void_p()
+        _check(lib().mlipg_create(os.fsencode(path), precision, ctypes.byref(h)))
+        self.h = h
+        self.precision = precision
+        v = (ctypes.c_longlong * 13)()
+        _check(lib().mlipg_model_info(self.h, v), self.h)
+        self.info = dict(zip(self.INFO, list(v)))
+        self.elements = [lib().mlipg_element_name(self.h, k).decode()
+                         for k in range(lib().mlipg_num_elements(self.h))]
+        self.masses = [lib().mlipg_element_mass(self.h, k) for k in range(len(self.elements))]
+        self.cutoff = lib().mlipg_cutoff(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mlipg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_precision(self, precision: int):
+        _check(lib().mlipg_set_precision(self.h, precision), self.h)
+        self.precision = precision
+
+    def set_type_map(self, names):
+        arr = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+        _check(lib().mlipg_set_type_map(self.h, len(names), arr), self.h)
+
+    def stream(self) -> int:
+        return lib().mlipg_stream(self.h) or 0
+
+    def itc_list(self):
+        n = lib().mlipg_dump_itc(self.h, None, 0)
+        b = np.zeros(n, dtype=np.int32)
+        lib().mlipg_dump_itc(self.h, _ip(b), n)
+        return b
+
+    def poly_list(self):
+        n = lib().mlipg_dump_poly(self.h, None, 0)
+        b = np.zeros(n, dtype=np.int32)
+        lib().mlipg_dump_poly(self.h, _ip(b), n)
+        return b
+
+    def flops_per_atom_step(self, elem: int, nbar: float) -> float:
+        return lib().mlipg_flops_per_atom_step(self.h, elem, nbar)
+
+    def compute_lammps(self, nlocal, nall, x, lmp_type, ilist, numneigh, firstneigh_arrays,
+                       eatom=True):
+        """LAMMPS-shaped call: x[nall,3], 1-based types, per-atom neighbour arrays.
+
+        Returns (energy, f_all[nall,3], virial6 LAMMPS order, eatom[nlocal]).
+        """
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        t = np.ascontiguousarray(lmp_type, dtype=np.int32)
+        il = np.ascontiguousarray(ilist, dtype=np.int32)
+        nn = np.ascontiguousarray(numneigh, dtype=np.int32)
+        keep = [np.ascontiguousarray(a, dtype=np.int32) for a in firstneigh_arrays]
+        fp = (ctypes.POINTER(ctypes.c_int) * max(nall, 1))()
+        for i, a in enumerate(keep):
+            fp[i] = _ip(a)
+        f = np.zeros((nall, 3))
+        e = ctypes.c_double()
+        vir = np.zeros(6)
+        ea = np.zeros(max(nlocal, 1)) if eatom else None
+        _check(lib().mlipg_compute(self.h, nlocal, nall, _dp(x), _ip(t), len(il), _ip(il),
+                                   _ip(nn), fp, 1, 1, _dp(f), ctypes.byref(e), _dp(vir),
+                                   _dp(ea) if eatom else None), self.h)
+        return e.value, f, vir, (ea[:nlocal] if eatom else None)
+
+    def compute(self, system, eatom=True):
+        """Evaluates a `structures.System` through the LAMMPS-shaped C ABI."""
+        off = system.nbr_off
+        lists = [system.nbr_idx[off[i]:off[i + 1]] for i in range(system.nlocal)]
+        nn = np.diff(off).astype(np.int32)
+        e, f, vir, ea = self.compute_lammps(system.nlocal, system.nall, system.x,
+                                            system.type + 1, np.arange(system.nlocal), nn, lists,
+                                            eatom)
+        return dict(energy=e, f_all=f, virial=vir, eatom=ea)
+
+    def compute_device(self, ncenters, x4, centers, nbr_off, nbr_idx, f, out8, eatom=None,
+                       img=None, cell=None, center_cell=None, fold=None, nb_cap=256):
+        """Stream-ordered call on device pointers (ints); see mlipg_compute_device."""
+        _check(lib().mlipg_compute_device(self.h, ncenters, x4, centers, nbr_off, nbr_idx,
+                                          img, cell, center_cell, fold, nb_cap, f, eatom, out8),
+               self.h)
+
+    def device_status(self) -> int:
+        b = ctypes.c_int()
+        _check(lib().mlipg_device_status(self.h, ctypes.byref(b)), self.h)
+        return b.value

@@ -1,0 +1,153 @@
+"""GPU path (through the C ABI) against the CPU oracle and the golden logs.
+
+Tolerances:
+* FP64 path: energy, every force component and the virial agree with the
+  oracle to 1e-10 relative (to the largest magnitude of each quantity);
+  only the summation order differs.
+* mixed path: energy error <= 1e-6 eV/atom on the synthetic workload
+  potentials and force RMS error <= 1e-4 eV/A against the FP64 oracle; on the
+  regression potentials (coefficients up to 1e5) the stated bound is a
+  relative one, 2e-5 of the force scale.
+"""
+import numpy as np
+import pytest
+
+import mlipg
+from conftest import structure
+from mlipg.potential import workload_potential
+from mlipg.structures import (bcc_cell, build_system, fcc_cell, jitter, random_triclinic_cell,
+                              random_types)
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-10
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def check_fp64(gpu, ref, sysm):
+    assert abs(gpu["energy"] - ref["energy"]) <= REL * abs(ref["energy"])
+    assert rel_err(gpu["f_all"], ref["f_all"]) <= REL
+    assert rel_err(gpu["virial"], ref["virial"]) <= REL
+    assert rel_err(gpu["eatom"], ref["eatom"]) <= REL
+    assert rel_err(sysm.fold_forces(gpu["f_all"]), sysm.fold_forces(ref["f_all"])) <= REL
+
+
+@pytest.fixture(scope="module")
+def ref_cache():
+    return {}
+
+
+@pytest.mark.parametrize("pot", ["gtinv-197", "gtinv-820", "gtinv-434"])
+def test_regression_potentials_fp64(potdir, golden, pot):
+    o = Oracle(potdir[pot], threads=16)
+    s = build_system(structure("structure.lammps"), o.cutoff, skin=2.0)
+    ref = o.compute(s)
+    g = mlipg.Potential(potdir[pot], mlipg.PREC_FP64)
+    got = g.compute(s)
+    check_fp64(got, ref, s)
+    gl = golden["thermo_step0"][pot]
+    assert got["energy"] == pytest.approx(gl["E_pair"], abs=6e-6)
+    assert s.pressure(got["virial"]) == pytest.approx(gl["Press"], abs=6e-4)
+
+
+def test_stress_and_triclinic_fp64(potdir, golden):
+    g = mlipg.Potential(potdir["gtinv-197"], mlipg.PREC_FP64)
+    s = build_system(structure("structure.lammps"), g.cutoff, skin=2.0)
+    p = s.pressure_tensor(g.compute(s)["virial"])
+    gl = golden["thermo_step0"]["gtinv-197-stress"]
+    np.testing.assert_allclose(p, [gl[k] for k in ["Pxx", "Pyy", "Pzz", "Pxy", "Pxz", "Pyz"]],
+                               atol=2e-3, rtol=0)
+    gc = golden["thermo_step0"]["gtinv-197-conv64"]
+    for name in ["structure_00064_conventional.lammps", "structure_00064_triclinic.lammps"]:
+        s = build_system(structure(name), g.cutoff, skin=2.0)
+        r = g.compute(s)
+        assert r["energy"] == pytest.approx(gc["E_pair"], abs=6e-6)
+        assert s.pressure(r["virial"]) == pytest.approx(gc["Press"], abs=0.1)
+
+
+@pytest.mark.parametrize("pot", ["gtinv-197", "gtinv-820", "gtinv-434"])
+def test_regression_potentials_mixed(potdir, pot):
+    o = Oracle(potdir[pot], threads=16)
+    s = build_system(structure("structure.lammps"), o.cutoff, skin=2.0)
+    ref = o.compute(s)
+    got = mlipg.Potential(potdir[pot], mlipg.PREC_MIXED).compute(s)
+    F, Fr = s.fold_forces(got["f_all"]), s.fold_forces(ref["f_all"])
+    scale = np.abs(Fr).max()
+    assert np.sqrt(np.mean((F - Fr) ** 2)) <= 2e-5 * scale
+    assert abs(got["energy"] - ref["energy"]) / s.nlocal <= 2e-5 * np.abs(ref["eatom"]).max()
+
+
+def workload_system(name, rng):
+    if name == "fcc-al-256":
+        cell = jitter(fcc_cell(4, 4, 4, 4.05), 0.05, rng)
+    elif name == "bcc-binary-16k":      # 3x3x3 bcc cell of the same alloy
+        cell = random_types(jitter(bcc_cell(3, 3, 3, 3.2), 0.05, rng), 2, rng)
+    elif name == "fcc-ternary-1m":      # 2x2x2 fcc cell of the same alloy
+        cell = random_types(jitter(fcc_cell(2, 2, 2, 4.0), 0.1, rng), 3, rng)
+    elif name == "triclinic-batch":
+        cell = random_triclinic_cell(24, 0.06, 2, rng)
+    return cell
+
+
+@pytest.mark.parametrize("name", ["fcc-al-256", "bcc-binary-16k", "fcc-ternary-1m",
+                                  "triclinic-batch"])
+def test_workload_potentials(tmp_path, name):
+    rng = np.random.default_rng(7)
+    path = str(tmp_path / (name + ".mlip"))
+    workload_potential(path, name, seed=3)
+    cell = workload_system(name, rng)
+    o = Oracle(path, threads=16)
+    s = build_system(cell, o.cutoff, skin=1.0)
+    ref = o.compute(s)
+    got = mlipg.Potential(path, mlipg.PREC_FP64).compute(s)
+    check_fp64(got, ref, s)
+    mix = mlipg.Potential(path, mlipg.PREC_MIXED).compute(s)
+    F, Fr = s.fold_forces(mix["f_all"]), s.fold_forces(ref["f_all"])
+    assert np.sqrt(np.mean((F - Fr) ** 2)) <= 1e-4
+    assert abs(mix["energy"] - ref["energy"]) / s.nlocal <= 1e-6
+
+
+def test_edge_cases(potdir):
+    g = mlipg.Potential(potdir["gtinv-820"], mlipg.PREC_FP64)
+    o = Oracle(potdir["gtinv-820"])
+    # empty system
+    e, f, vir, ea = g.compute_lammps(0, 0, np.zeros((0, 3)), [], [], [], [])
+    assert e == 0.0 and np.all(vir == 0)
+    # isolated atoms (no neighbours inside the cutoff) and a NULL-mapped type
+    cell = structure("structure.lammps")
+    s = build_system(cell, g.cutoff, skin=2.0)
+    g.set_type_map(["Ti", "Al", "NULL"])
+    t = s.type.copy() + 1
+    t[5] = 3                       # atom 5 (and its images) not handled by this style
+    t[s.owner == 5] = 3
+    off = s.nbr_off
+    lists = [s.nbr_idx[off[i]:off[i + 1]] for i in range(s.nlocal)]
+    e, f, vir, ea = g.compute_lammps(s.nlocal, s.nall, s.x, t, np.arange(s.nlocal),
+                                     np.diff(off), lists)
+    assert ea[5] == 0.0
+    tt = s.type.copy()
+    tt[s.owner == 5] = -1
+    s2 = type(s)(**{**s.__dict__, "type": tt})
+    ref = o.compute(s2)
+    assert abs(e - ref["energy"]) <= REL * abs(ref["energy"])
+    assert rel_err(f, ref["f_all"]) <= REL
+    # a subset of centres via ilist
+    g.set_type_map(["Ti", "Al"])
+    il = np.arange(0, s.nlocal, 3)
+    e2, f2, _, ea2 = g.compute_lammps(s.nlocal, s.nall, s.x, s.type + 1, il, np.diff(off), lists)
+    full = o.compute(s)
+    assert e2 == pytest.approx(full["eatom"][il].sum(), rel=1e-10)
+
+
+def test_repeatability(potdir):
+    g = mlipg.Potential(potdir["gtinv-820"], mlipg.PREC_MIXED)
+    s = build_system(structure("structure.lammps"), g.cutoff, skin=2.0)
+    a = g.compute(s)
+    b = g.compute(s)
+    assert a["energy"] == b["energy"]
+    np.testing.assert_allclose(a["f_all"], b["f_all"], rtol=0, atol=1e-12)
