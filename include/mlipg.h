@@ -134,6 +134,33 @@ long mlipg_dump_poly(const mlipg_handle* h, int* out, long cap);
 /* Algorithmic FLOPs per atom step for element `elem` with nbar neighbours. */
 double mlipg_flops_per_atom_step(const mlipg_handle* h, int elem, double nbar);
 
+/* Per-launch device time of the fused kernel: when on, every launch is
+ * bracketed by CUDA events on the handle's stream; mlipg_kernel_times copies
+ * the durations (ms) of the launches since the last call and clears them.
+ * Returns the number copied.  Measurement support; no reference counterpart. */
+int mlipg_set_profiling(mlipg_handle* h, int on);
+int mlipg_kernel_times(mlipg_handle* h, float* ms, int cap);
+
+/* Live FMA throughput of the CUDA-core FP32 (fp64 = 0) or FP64 (fp64 = 1)
+ * pipe on the current device, in TFLOP/s: the roofline denominator of the
+ * fused kernel.  Measurement support; no reference counterpart. */
+int mlipg_measure_fma_peak(int fp64, double* tflops);
+
+/* Host neighbour-list builder for standalone and batched use: owned atoms
+ * (wrapped into the cell), ghost images within `cutoff` in fractional
+ * coordinates (LAMMPS's ghost rule for triclinic boxes), each atom's owner
+ * and packed image code, and a full list (distance < cutoff) of the owned
+ * atoms in CSR form.  lattice9 holds the cell vectors a1, a2, a3 as rows.
+ * Replaces get_neighbors (src/USER-MLIP/mlipkk_cell.cpp:218-307), which
+ * returns a half list of displacements instead. */
+typedef struct mlipg_nlist mlipg_nlist;
+int mlipg_nlist_build(const double* lattice9, int natoms, const double* x, const int* type,
+                      double cutoff, mlipg_nlist** out);
+int mlipg_nlist_sizes(const mlipg_nlist* nl, int* nall, long long* npairs);
+int mlipg_nlist_copy(const mlipg_nlist* nl, double* x_all, int* type_all, int* owner,
+                     int* image, int* nbr_off, int* nbr_idx);
+void mlipg_nlist_destroy(mlipg_nlist* nl);
+
 #ifdef __cplusplus
 }
 #endif

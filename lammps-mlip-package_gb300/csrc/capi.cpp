@@ -87,6 +87,10 @@ struct mlipg_handle {
   DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_partials, d_status, d_out8;
   HostBuf h_x4, h_centers, h_off, h_idx, h_f, h_eatom, h_out;
   int last_status = 0;
+  // per-launch timing of the fused kernel (measurement support)
+  bool profiling = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
+  std::vector<cudaEvent_t> ev_pool;
 };
 
 static int fail(mlipg_handle* h, int code, const char* fmt, ...) {
@@ -222,6 +226,8 @@ int mlipg_destroy(mlipg_handle* h) {
                     &h->d_centers, &h->d_off, &h->d_idx, &h->d_f, &h->d_eatom, &h->d_partials,
                     &h->d_status, &h->d_out8};
   for (DevBuf* b : bufs) b->release();
+  for (auto& pr : h->ev_pending) h->ev_pool.insert(h->ev_pool.end(), {pr.first, pr.second});
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   HostBuf* hb[] = {&h->h_x4, &h->h_centers, &h->h_off, &h->h_idx, &h->h_f, &h->h_eatom,
                    &h->h_out};
   for (HostBuf* b : hb) b->release();
@@ -336,7 +342,23 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.eatom = eatom;
   a.partials = h->d_partials.as<double>();
   a.status = h->d_status.as<int>();
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (h->profiling && ncenters > 0) {
+    for (cudaEvent_t* ev : {&ev0, &ev1}) {
+      if (!h->ev_pool.empty()) {
+        *ev = h->ev_pool.back();
+        h->ev_pool.pop_back();
+      } else {
+        CK(cudaEventCreate(ev), "event create");
+      }
+    }
+    CK(cudaEventRecord(ev0, h->stream), "event record");
+  }
   if (ncenters > 0) CK(launch_fused(fp64, M.L, a, grid, smem, h->stream), "fused kernel launch");
+  if (ev0) {
+    CK(cudaEventRecord(ev1, h->stream), "event record");
+    h->ev_pending.push_back({ev0, ev1});
+  }
   else CK(cudaMemsetAsync(a.partials, 0, 8 * sizeof(double), h->stream), "memset partials");
   CK(launch_finalize(a.partials, ncenters > 0 ? grid : 1, out8, h->stream), "finalize launch");
   return MLIPG_OK;
@@ -374,6 +396,7 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
   // pack positions and element indices
   CK(h->h_x4.reserve((size_t)std::max(nall, 1) * sizeof(double4)), "pinned x4");
   double4* hx = h->h_x4.as<double4>();
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nall; ++i) {
     const int t = type[i];
     const int e = (t >= 1 && t <= ntypes) ? h->type_map[t] : -1;
@@ -399,16 +422,19 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
   }
   CK(h->h_idx.reserve((size_t)std::max<long long>(np, 1) * sizeof(int)), "pinned neighbours");
   int* hi = h->h_idx.as<int>();
+  int bad = -1;
+#pragma omp parallel for schedule(dynamic, 1024)
   for (int c = 0; c < nc; ++c) {
     const int i = hc[c];
     const int* jl = firstneigh[i];
     int* dst = hi + ho[c];
     for (int jj = 0; jj < numneigh[i]; ++jj) {
       const int j = jl[jj] & kNeighMask;
-      if (j < 0 || j >= nall) return fail(h, MLIPG_EINVAL, "neighbour index %d outside nall", j);
+      if (j < 0 || j >= nall) bad = j;
       dst[jj] = j;
     }
   }
+  if (bad != -1) return fail(h, MLIPG_EINVAL, "neighbour index %d outside nall", bad);
   // upload
   cudaStream_t s = h->stream;
   CK(h->d_x4.reserve((size_t)std::max(nall, 1) * sizeof(double4)), "alloc x4");
@@ -457,7 +483,9 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
                 std::max(32, std::min(kNbCapMax, (maxn + 31) / 32 * 32)));
   if (status & kStatusBadType) return fail(h, MLIPG_EINVAL, "element index out of range");
   const double* hf = h->h_f.as<double>();
-  for (size_t k = 0; k < (size_t)nall * 3; ++k) f[k] += hf[k];
+  const long long nf = (long long)nall * 3;
+#pragma omp parallel for schedule(static)
+  for (long long k = 0; k < nf; ++k) f[k] += hf[k];
   const double* o = h->h_out.as<double>();
   if (eflag) *energy = o[0];
   if (vflag) {
@@ -474,6 +502,29 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
     for (int c = 0; c < nc; ++c) eatom[hc[c]] += he[c];
   }
   return MLIPG_OK;
+}
+
+extern "C" int mlipg_set_profiling(mlipg_handle* h, int on) {
+  if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
+  h->profiling = on != 0;
+  return MLIPG_OK;
+}
+
+extern "C" int mlipg_kernel_times(mlipg_handle* h, float* ms, int cap) {
+  if (!h || (cap > 0 && !ms)) return -1;
+  int n = 0;
+  for (auto& pr : h->ev_pending) {
+    if (n < cap) {
+      if (cudaEventSynchronize(pr.second) != cudaSuccess ||
+          cudaEventElapsedTime(ms + n, pr.first, pr.second) != cudaSuccess)
+        ms[n] = -1.0f;
+      ++n;
+    }
+    h->ev_pool.push_back(pr.first);
+    h->ev_pool.push_back(pr.second);
+  }
+  h->ev_pending.clear();
+  return n;
 }
 
 extern "C" int mlipg_count_coefficients(int n_types, int model_type, int maxp, int maxl,

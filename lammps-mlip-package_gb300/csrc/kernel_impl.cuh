@@ -548,11 +548,9 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
     // ---------------------------------------------------------------- P5
     {
       const int u0 = __ldg(A.unit_off + ti), nU = __ldg(A.unit_off + ti + 1) - u0;
-      while (true) {
-        int u = 0;
-        if (lane == 0) u = atomicAdd(misc + 10, 1);
-        u = __shfl_sync(0xffffffffu, u, 0);
-        if (u >= nU) break;
+      // static round-robin over warps (units are sorted by cost): each
+      // thread's energy sum has a fixed order, so energies are reproducible
+      for (int u = warp; u < nU; u += kBlock / 32) {
         const DeviceUnit un = A.units[u0 + u];
         double hv = 0.0;
         if (act) {

@@ -62,6 +62,13 @@ def lib():
         "mlipg_dump_itc": (ctypes.c_long, [P, ip, ctypes.c_long]),
         "mlipg_dump_poly": (ctypes.c_long, [P, ip, ctypes.c_long]),
         "mlipg_flops_per_atom_step": (ctypes.c_double, [P, i32, ctypes.c_double]),
+        "mlipg_nlist_build": (i32, [dp, i32, dp, ip, ctypes.c_double, ctypes.POINTER(P)]),
+        "mlipg_nlist_sizes": (i32, [P, ip, llp]),
+        "mlipg_nlist_copy": (i32, [P, dp, ip, ip, ip, ip, ip]),
+        "mlipg_nlist_destroy": (None, [P]),
+        "mlipg_set_profiling": (i32, [P, i32]),
+        "mlipg_kernel_times": (i32, [P, ctypes.POINTER(ctypes.c_float), i32]),
+        "mlipg_measure_fma_peak": (i32, [i32, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -95,6 +102,41 @@ def count_coefficients(n_types, model_type, maxp, maxl, gtinv_order, gtinv_maxl,
     _check(lib().mlipg_count_coefficients(n_types, model_type, maxp, maxl, gtinv_order, _ip(ml),
                                           _ip(sy), n_fn, ctypes.byref(nc), ctypes.byref(nf)))
     return nc.value, nf.value
+
+
+def measure_fma_peak(fp64: bool) -> float:
+    """Live FP64 / FP32 CUDA-core FMA throughput of the current device (TFLOP/s)."""
+    v = ctypes.c_double()
+    _check(lib().mlipg_measure_fma_peak(1 if fp64 else 0, ctypes.byref(v)))
+    return v.value
+
+
+def native_system(cell, cutoff: float, skin: float = 0.0):
+    """`structures.System` built by the library's native neighbour builder."""
+    from .structures import Cell, System
+    lat = np.ascontiguousarray(cell.lattice, dtype=np.float64)
+    x = np.ascontiguousarray(cell.positions, dtype=np.float64)
+    t = np.ascontiguousarray(cell.types, dtype=np.int32)
+    h = ctypes.c_void_p()
+    _check(lib().mlipg_nlist_build(_dp(lat), len(t), _dp(x), _ip(t), cutoff + skin,
+                                   ctypes.byref(h)))
+    try:
+        nall = ctypes.c_int()
+        npairs = ctypes.c_longlong()
+        _check(lib().mlipg_nlist_sizes(h, ctypes.byref(nall), ctypes.byref(npairs)))
+        xa = np.zeros((nall.value, 3))
+        ta = np.zeros(nall.value, dtype=np.int32)
+        ow = np.zeros(nall.value, dtype=np.int32)
+        im = np.zeros(nall.value, dtype=np.int32)
+        off = np.zeros(len(t) + 1, dtype=np.int32)
+        idx = np.zeros(max(npairs.value, 1), dtype=np.int32)
+        _check(lib().mlipg_nlist_copy(h, _dp(xa), _ip(ta), _ip(ow), _ip(im), _ip(off), _ip(idx)))
+    finally:
+        lib().mlipg_nlist_destroy(h)
+    s = System(cell=Cell(lat, xa[:len(t)].copy(), t), x=xa, type=ta, owner=ow.astype(np.int64),
+               nbr_off=off, nbr_idx=idx[:npairs.value], nlocal=len(t), cutoff=cutoff)
+    s.image = im
+    return s
 
 
 class Potential:
@@ -189,6 +231,14 @@ class Potential:
         _check(lib().mlipg_compute_device(self.h, ncenters, x4, centers, nbr_off, nbr_idx,
                                           img, cell, center_cell, fold, nb_cap, f, eatom, out8),
                self.h)
+
+    def set_profiling(self, on: bool):
+        _check(lib().mlipg_set_profiling(self.h, 1 if on else 0), self.h)
+
+    def kernel_times(self, cap: int = 4096):
+        buf = (ctypes.c_float * cap)()
+        n = lib().mlipg_kernel_times(self.h, buf, cap)
+        return [buf[k] for k in range(max(n, 0))]
 
     def device_status(self) -> int:
         b = ctypes.c_int()

@@ -46,7 +46,9 @@ def _sources():
     return {
         "model.o": ("g++", os.path.join(CSRC, "model.cpp")),
         "capi.o": ("g++", os.path.join(CSRC, "capi.cpp")),
+        "neighbor.o": ("g++", os.path.join(CSRC, "neighbor.cpp")),
         "kernels_common.o": ("nvcc", os.path.join(CSRC, "kernels_common.cu")),
+        "peak.o": ("nvcc", os.path.join(CSRC, "peak.cu")),
         "kernels_f64.o": ("nvcc", os.path.join(CSRC, "kernels_f64.cu")),
         "kernels_f32.o": ("nvcc", os.path.join(CSRC, "kernels_f32.cu")),
     }
@@ -73,7 +75,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for obj, (tool, src) in _sources().items():
         out = os.path.join(OUT_DIR, obj)
         if tool == "g++":
-            cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-Wall", "-c", src, "-o", out] + inc
+            cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-Wall", "-c", src, "-o",
+                   out] + inc
         else:
             cmd = [nvcc] + ARCH + ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
                                    "-c", src, "-o", out] + inc
@@ -93,7 +96,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = [os.path.join(OUT_DIR, o) for o in _sources()]
     tmp = LIB + ".tmp"
     subprocess.check_call([nvcc] + ARCH + ["-shared", "-o", tmp] + objs +
-                          ["-lcudart_static", "-lrt", "-lpthread", "-ldl"])
+                          ["-lcudart_static", "-lrt", "-lpthread", "-ldl", "-lgomp"])
     os.replace(tmp, LIB)
     return LIB
 
