@@ -354,12 +354,15 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
     }
     CK(cudaEventRecord(ev0, h->stream), "event record");
   }
-  if (ncenters > 0) CK(launch_fused(fp64, M.L, a, grid, smem, h->stream), "fused kernel launch");
+  if (ncenters > 0) {
+    CK(launch_fused(fp64, M.L, a, grid, smem, h->stream), "fused kernel launch");
+  } else {
+    CK(cudaMemsetAsync(a.partials, 0, 8 * sizeof(double), h->stream), "memset partials");
+  }
   if (ev0) {
     CK(cudaEventRecord(ev1, h->stream), "event record");
     h->ev_pending.push_back({ev0, ev1});
   }
-  else CK(cudaMemsetAsync(a.partials, 0, 8 * sizeof(double), h->stream), "memset partials");
   CK(launch_finalize(a.partials, ncenters > 0 ? grid : 1, out8, h->stream), "finalize launch");
   return MLIPG_OK;
 }
@@ -583,3 +586,4 @@ extern "C" double mlipg_flops_per_atom_step(const mlipg_handle* h, int elem, dou
   if (!h || elem < 0 || elem >= h->model.T) return 0.0;
   return flops_per_atom_step(h->model, elem, nbar);
 }
+

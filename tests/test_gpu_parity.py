@@ -151,3 +151,38 @@ def test_repeatability(potdir):
     b = g.compute(s)
     assert a["energy"] == b["energy"]
     np.testing.assert_allclose(a["f_all"], b["f_all"], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("ncent", [1, 2, 32])
+def test_device_api_totals_match_per_atom(potdir, ncent):
+    """out8 (energy, virial) of mlipg_compute_device equals the per-atom sums."""
+    import torch
+    g = mlipg.Potential(potdir["gtinv-820"], mlipg.PREC_FP64)
+    s = build_system(structure("structure.lammps"), g.cutoff, skin=2.0)
+    dev = torch.device("cuda")
+    x4 = np.zeros((s.nall, 4))
+    x4[:, :3] = s.x
+    x4[:, 3] = s.type
+    cents = list(range(ncent))
+    offs = np.zeros(ncent + 1, dtype=np.int32)
+    idx = []
+    for k, i in enumerate(cents):
+        lst = s.nbr_idx[s.nbr_off[i]:s.nbr_off[i + 1]]
+        idx.append(lst)
+        offs[k + 1] = offs[k] + len(lst)
+    t = {k: torch.from_numpy(v).to(dev) for k, v in
+         dict(x4=x4, c=np.array(cents, np.int32), o=offs, i=np.concatenate(idx)).items()}
+    f = torch.zeros((s.nall, 3), dtype=torch.float64, device=dev)
+    out = torch.full((8,), -7.0, dtype=torch.float64, device=dev)
+    ea = torch.zeros(ncent, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        g.compute_device(ncent, t["x4"].data_ptr(), t["c"].data_ptr(), t["o"].data_ptr(),
+                         t["i"].data_ptr(), f.data_ptr(), out.data_ptr(), eatom=ea.data_ptr(),
+                         nb_cap=512)
+    torch.cuda.synchronize()
+    ref = Oracle(potdir["gtinv-820"]).compute_centers(s, np.array(cents))
+    assert out[0].item() == pytest.approx(ea.sum().item(), rel=1e-12)
+    assert out[0].item() == pytest.approx(ref["energy"], rel=1e-10)
+    v = out.cpu().numpy()[1:7]
+    # kernel order xx yy zz yz zx xy vs oracle's LAMMPS order xx yy zz xy xz yz
+    np.testing.assert_allclose(v[[0, 1, 2, 5, 4, 3]], ref["virial"], rtol=1e-9, atol=1e-12)
