@@ -302,7 +302,8 @@ def run_ours(args, dist):
     def e2e_step():
         fh[:] = 0.0
         rcode = L.mlipg_compute(g.h, natoms, sysm.nall, dp(xh), ip(ltype), natoms, ip(ilist),
-                                ip(numneigh), fp, 1, 1, dp(fh), ctypes.byref(e), dp(vir), None)
+                                ip(numneigh), fp, 1, 1, dp(fh), ctypes.byref(e), dp(vir), None,
+                                None)
         if rcode != 0:
             raise RuntimeError(L.mlipg_last_error(g.h).decode())
 

@@ -82,14 +82,17 @@ int mlipg_set_type_map(mlipg_handle* h, int n_lmp_types, const char* const* elem
  *   inum/ilist/numneigh/firstneigh (entries masked with NEIGHMASK).
  * Outputs: f[nall*3] is ACCUMULATED (ghost forces included, to be reverse-
  * communicated as LAMMPS does); *energy and virial[6] are overwritten when
- * eflag / vflag are non-zero; eatom[nlocal] is accumulated if not NULL.
+ * eflag / vflag are non-zero; eatom[nlocal] and vatom[nlocal][6] (LAMMPS order)
+ * are accumulated if not NULL.  Per-atom virials attribute each pair's
+ * -r_ij (x) f_ij to the atom whose adjoint produced f_ij (the reference
+ * allocates but never fills eatom/vatom, pair_mlip_gtinv_kokkos_impl.h:287-296).
  * Replaces PairMLIPGtinvKokkos::compute (pair_mlip_gtinv_kokkos_impl.h:272-406)
  * with set_structure (:411-599), MLIPModelLMP::compute (mlipkk_lmp.h:145-228),
  * get_forces (:601-634) and get_stress (mlipkk_lmp.h:942-955). */
 int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double* x, const int* type,
                   int inum, const int* ilist, const int* numneigh, const int* const* firstneigh,
                   int eflag, int vflag, double* f, double* energy, double* virial,
-                  double* eatom);
+                  double* eatom, double* vatom);
 
 /* Same evaluation on device-resident data, stream-ordered on the handle's
  * stream (no host synchronisation; capturable in a CUDA graph).
@@ -99,14 +102,16 @@ int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double* x, const 
  *     code = (n1+512) | (n2+512)<<10 | (n3+512)<<20, 0 = no shift, applied
  *     with the lattice rows d_cell[9*d_center_cell[c]] of the centre's cell;
  *   d_fold (optional, NULL): atom -> force row (ghost -> owner).
- *   d_f[nforce*3] accumulated; d_eatom[ncenters] written (optional);
+ *   d_f[nforce*3] accumulated; d_eatom[ncenters] and d_vatom[ncenters][6]
+ *   (LAMMPS order) written (optional);
  *   d_out8: [energy, virial xx yy zz xy xz yz, spare] written.
  * No counterpart in the reference (its device stages are internal,
  * mlipkk_lmp.h:145-228); this is the entry used by MD loops and batching. */
 int mlipg_compute_device(mlipg_handle* h, int ncenters, const void* d_x4, const int* d_centers,
                          const int* d_nbr_off, const int* d_nbr_idx, const int* d_img,
                          const double* d_cell, const int* d_center_cell, const int* d_fold,
-                         int nb_cap, double* d_f, double* d_eatom, double* d_out8);
+                         int nb_cap, double* d_f, double* d_eatom, double* d_vatom,
+                         double* d_out8);
 
 /* The handle's CUDA stream (cudaStream_t) for ordering caller work. */
 void* mlipg_stream(mlipg_handle* h);

@@ -84,7 +84,7 @@ struct mlipg_handle {
   // model tables on the device
   DevBuf d_terms, d_units, d_unit_off, d_nl, d_nl_off, d_poly, d_poly_off, d_wlin, d_radial;
   // per-call buffers (grow only)
-  DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_partials, d_status, d_out8;
+  DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_vatom, d_partials, d_status, d_out8;
   HostBuf h_x4, h_centers, h_off, h_idx, h_f, h_eatom, h_out;
   int last_status = 0;
   // per-launch timing of the fused kernel (measurement support)
@@ -223,7 +223,7 @@ int mlipg_destroy(mlipg_handle* h) {
   }
   DevBuf* bufs[] = {&h->d_terms, &h->d_units, &h->d_unit_off, &h->d_nl, &h->d_nl_off,
                     &h->d_poly, &h->d_poly_off, &h->d_wlin, &h->d_radial, &h->d_x4,
-                    &h->d_centers, &h->d_off, &h->d_idx, &h->d_f, &h->d_eatom, &h->d_partials,
+                    &h->d_centers, &h->d_off, &h->d_idx, &h->d_f, &h->d_eatom, &h->d_vatom, &h->d_partials,
                     &h->d_status, &h->d_out8};
   for (DevBuf* b : bufs) b->release();
   for (auto& pr : h->ev_pending) h->ev_pool.insert(h->ev_pool.end(), {pr.first, pr.second});
@@ -295,7 +295,7 @@ int mlipg_device_status(mlipg_handle* h, int* bits) {
 static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const int* centers,
                       const int* off, const int* idx, const int* img, const double* cell,
                       const int* center_cell, const int* fold, int nb_cap, double* f,
-                      double* eatom, double* out8) {
+                      double* eatom, double* vatom, double* out8) {
   const Model& M = h->model;
   const bool fp64 = h->precision == MLIPG_PREC_FP64;
   nb_cap = std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
@@ -340,6 +340,7 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.rc = M.pot.cutoff;
   a.f = f;
   a.eatom = eatom;
+  a.vatom = vatom;
   a.partials = h->d_partials.as<double>();
   a.status = h->d_status.as<int>();
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -371,7 +372,8 @@ extern "C" int mlipg_compute_device(mlipg_handle* h, int ncenters, const void* d
                                     const int* d_centers, const int* d_nbr_off,
                                     const int* d_nbr_idx, const int* d_img, const double* d_cell,
                                     const int* d_center_cell, const int* d_fold, int nb_cap,
-                                    double* d_f, double* d_eatom, double* d_out8) {
+                                    double* d_f, double* d_eatom, double* d_vatom,
+                                    double* d_out8) {
   if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
   if (h->device < 0) return fail(h, MLIPG_ENOGPU, "no CUDA device is available");
   if (ncenters < 0 || (ncenters > 0 && (!d_x4 || !d_centers || !d_nbr_off || !d_nbr_idx)) ||
@@ -381,13 +383,13 @@ extern "C" int mlipg_compute_device(mlipg_handle* h, int ncenters, const void* d
     return fail(h, MLIPG_EINVAL, "image codes need the cell lattices and centre cell ids");
   return run_kernel(h, ncenters, static_cast<const double4*>(d_x4), d_centers, d_nbr_off,
                     d_nbr_idx, d_img, d_cell, d_center_cell, d_fold, nb_cap, d_f, d_eatom,
-                    d_out8);
+                    d_vatom, d_out8);
 }
 
 extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double* x,
                              const int* type, int inum, const int* ilist, const int* numneigh,
                              const int* const* firstneigh, int eflag, int vflag, double* f,
-                             double* energy, double* virial, double* eatom) {
+                             double* energy, double* virial, double* eatom, double* vatom) {
   if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
   if (h->device < 0) return fail(h, MLIPG_ENOGPU, "no CUDA device is available");
   if (nlocal < 0 || nall < nlocal || inum < 0 || (nall > 0 && (!x || !type)) ||
@@ -446,6 +448,7 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
   CK(h->d_idx.reserve((size_t)std::max<long long>(np, 1) * sizeof(int)), "alloc neighbours");
   CK(h->d_f.reserve((size_t)std::max(nall, 1) * 3 * sizeof(double)), "alloc forces");
   CK(h->d_eatom.reserve((size_t)std::max(nc, 1) * sizeof(double)), "alloc eatom");
+  CK(h->d_vatom.reserve((size_t)std::max(nc, 1) * 6 * sizeof(double)), "alloc vatom");
   CK(h->d_out8.reserve(8 * sizeof(double)), "alloc out");
   CK(cudaMemcpyAsync(h->d_x4.p, hx, (size_t)nall * sizeof(double4), cudaMemcpyHostToDevice, s),
      "copy x4");
@@ -459,11 +462,12 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
   CK(cudaMemsetAsync(h->d_f.p, 0, (size_t)nall * 3 * sizeof(double), s), "memset forces");
   int rc = run_kernel(h, nc, h->d_x4.as<double4>(), h->d_centers.as<int>(), h->d_off.as<int>(),
                       h->d_idx.as<int>(), nullptr, nullptr, nullptr, nullptr, maxn,
-                      h->d_f.as<double>(), h->d_eatom.as<double>(), h->d_out8.as<double>());
+                      h->d_f.as<double>(), h->d_eatom.as<double>(),
+                      vatom ? h->d_vatom.as<double>() : nullptr, h->d_out8.as<double>());
   if (rc != MLIPG_OK) return rc;
   // download
   CK(h->h_f.reserve((size_t)std::max(nall, 1) * 3 * sizeof(double)), "pinned forces");
-  CK(h->h_eatom.reserve((size_t)std::max(nc, 1) * sizeof(double)), "pinned eatom");
+  CK(h->h_eatom.reserve((size_t)std::max(nc, 1) * 7 * sizeof(double)), "pinned eatom");
   CK(h->h_out.reserve(16 * sizeof(double)), "pinned out");
   CK(cudaMemcpyAsync(h->h_f.p, h->d_f.p, (size_t)nall * 3 * sizeof(double),
                      cudaMemcpyDeviceToHost, s),
@@ -472,6 +476,10 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
     CK(cudaMemcpyAsync(h->h_eatom.p, h->d_eatom.p, (size_t)nc * sizeof(double),
                        cudaMemcpyDeviceToHost, s),
        "copy eatom");
+  if (vatom)
+    CK(cudaMemcpyAsync(h->h_eatom.as<double>() + nc, h->d_vatom.p, (size_t)nc * 6 * sizeof(double),
+                       cudaMemcpyDeviceToHost, s),
+       "copy vatom");
   CK(cudaMemcpyAsync(h->h_out.p, h->d_out8.p, 8 * sizeof(double), cudaMemcpyDeviceToHost, s),
      "copy energy");
   CK(cudaMemcpyAsync(h->h_out.as<double>() + 8, h->d_status.p, sizeof(int),
@@ -503,6 +511,11 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
   if (eatom) {
     const double* he = h->h_eatom.as<double>();
     for (int c = 0; c < nc; ++c) eatom[hc[c]] += he[c];
+  }
+  if (vatom) {
+    const double* hv = h->h_eatom.as<double>() + nc;
+    for (int c = 0; c < nc; ++c)
+      for (int k = 0; k < 6; ++k) vatom[6 * (size_t)hc[c] + k] += hv[6 * (size_t)c + k];
   }
   return MLIPG_OK;
 }

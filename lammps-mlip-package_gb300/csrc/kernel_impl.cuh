@@ -349,7 +349,7 @@ __host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int
   s.nbk = s.hnl + align16((size_t)nl_cap * kNPad * sizeof(double));
   s.misc = s.nbk + align16((size_t)nb_cap * sizeof(int));
   s.red = s.misc + align16(32 * sizeof(int));
-  s.total = s.red + align16(8 * (kBlock / 32) * sizeof(double));
+  s.total = s.red + align16(16 * (kBlock / 32) * sizeof(double));
   return s;
 }
 
@@ -566,6 +566,7 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
     __syncthreads();
     // ---------------------------------------------------------------- P6
     double fix = 0.0, fiy = 0.0, fiz = 0.0;
+    double va[6] = {0, 0, 0, 0, 0, 0};   // this centre's virial (reference order)
     for (int jj = tid; jj < nkeep; jj += kBlock) {
       const int k = nbk[jj];
       const int j = __ldg(A.nbr_idx + k);
@@ -587,20 +588,31 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
       atomicAdd(A.f + 3 * (size_t)fj + 1, -fy);
       atomicAdd(A.f + 3 * (size_t)fj + 2, -fz);
       // reference component order: xx yy zz yz zx xy
-      vir[0] -= dx * fx; vir[1] -= dy * fy; vir[2] -= dz * fz;
-      vir[3] -= dy * fz; vir[4] -= dz * fx; vir[5] -= dx * fy;
+      va[0] -= dx * fx; va[1] -= dy * fy; va[2] -= dz * fz;
+      va[3] -= dy * fz; va[4] -= dz * fx; va[5] -= dx * fy;
     }
-    // block reduction of the centre's energy and force
-    double s0 = warp_sum(eacc), s1 = warp_sum(fix), s2 = warp_sum(fiy), s3 = warp_sum(fiz);
-    if (lane == 0) {
-      red[warp * 4 + 0] = s0; red[warp * 4 + 1] = s1;
-      red[warp * 4 + 2] = s2; red[warp * 4 + 3] = s3;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) vir[q] += va[q];
+    // block reduction of the centre's energy, force and virial
+    {
+      double v10[10] = {eacc, fix, fiy, fiz, va[0], va[1], va[2], va[3], va[4], va[5]};
+#pragma unroll
+      for (int q = 0; q < 10; ++q) v10[q] = warp_sum(v10[q]);
+      if (lane == 0)
+        for (int q = 0; q < 10; ++q) red[warp * 16 + q] = v10[q];
     }
     __syncthreads();
+    if (tid < 6 && A.vatom) {
+      double v = 0;
+      for (int w = 0; w < kBlock / 32; ++w) v += red[w * 16 + 4 + tid];
+      // reference order xx yy zz yz zx xy -> LAMMPS xx yy zz xy xz yz
+      const int dst = tid < 3 ? tid : (tid == 3 ? 5 : (tid == 4 ? 4 : 3));
+      A.vatom[(size_t)c * 6 + dst] = v;
+    }
     if (tid == 0) {
       double e = 0, gx = 0, gy = 0, gz = 0;
       for (int w = 0; w < kBlock / 32; ++w) {
-        e += red[w * 4]; gx += red[w * 4 + 1]; gy += red[w * 4 + 2]; gz += red[w * 4 + 3];
+        e += red[w * 16]; gx += red[w * 16 + 1]; gy += red[w * 16 + 2]; gz += red[w * 16 + 3];
       }
       if (A.eatom) A.eatom[c] = e;
       ecta += e;
@@ -617,11 +629,11 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
   for (int q = 0; q < 7; ++q) vals[q] = warp_sum(vals[q]);
   __syncthreads();
   if (lane == 0)
-    for (int q = 0; q < 7; ++q) red[warp * 8 + q] = vals[q];
+    for (int q = 0; q < 7; ++q) red[warp * 16 + q] = vals[q];
   __syncthreads();
   if (tid < 7) {
     double s = 0;
-    for (int w = 0; w < kBlock / 32; ++w) s += red[w * 8 + tid];
+    for (int w = 0; w < kBlock / 32; ++w) s += red[w * 16 + tid];
     A.partials[(size_t)blockIdx.x * 8 + tid] = s;
   }
 }

@@ -43,6 +43,7 @@ struct KernelArgs {
   // outputs
   double* f;              // [nforce][3], accumulated with atomics
   double* eatom;          // [ncenters] (may be null)
+  double* vatom;          // [ncenters][6] centre virial, LAMMPS order xx yy zz xy xz yz (may be null)
   double* partials;       // [gridDim.x][8]: energy, virial(6, reference order), spare
   int* status;            // [1]
 };

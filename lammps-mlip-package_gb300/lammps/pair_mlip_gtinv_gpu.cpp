@@ -119,7 +119,8 @@ void PairMLIPGtinvGPU::compute(int eflag, int vflag)
   const int rc = mlipg_compute(handle, nlocal, nall, &atom->x[0][0], atom->type, list->inum,
                                list->ilist, list->numneigh, list->firstneigh, eflag_global,
                                vflag_global, &atom->f[0][0], &energy, vir,
-                               eflag_atom ? eatom : nullptr);
+                               eflag_atom ? eatom : nullptr,
+                               vflag_atom ? &vatom[0][0] : nullptr);
   if (rc != MLIPG_OK) error->one(FLERR, mlipg_last_error(handle));
   if (eflag_global) eng_vdwl += energy;
   if (vflag_global)

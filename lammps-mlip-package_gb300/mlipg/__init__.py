@@ -53,8 +53,8 @@ def lib():
         "mlipg_cutoff": (ctypes.c_double, [P]),
         "mlipg_set_type_map": (i32, [P, i32, ctypes.POINTER(ctypes.c_char_p)]),
         "mlipg_compute": (i32, [P, i32, i32, dp, ip, i32, ip, ip, ctypes.POINTER(ip), i32, i32,
-                                dp, dp, dp, dp]),
-        "mlipg_compute_device": (i32, [P, i32, P, P, P, P, P, P, P, P, i32, P, P, P]),
+                                dp, dp, dp, dp, dp]),
+        "mlipg_compute_device": (i32, [P, i32, P, P, P, P, P, P, P, P, i32, P, P, P, P]),
         "mlipg_stream": (P, [P]),
         "mlipg_device_status": (i32, [P, ip]),
         "mlipg_count_coefficients": (i32, [i32, i32, i32, i32, i32, ip, ip, i32, llp, llp]),
@@ -193,10 +193,11 @@ class Potential:
         return lib().mlipg_flops_per_atom_step(self.h, elem, nbar)
 
     def compute_lammps(self, nlocal, nall, x, lmp_type, ilist, numneigh, firstneigh_arrays,
-                       eatom=True):
+                       eatom=True, vatom=False):
         """LAMMPS-shaped call: x[nall,3], 1-based types, per-atom neighbour arrays.
 
-        Returns (energy, f_all[nall,3], virial6 LAMMPS order, eatom[nlocal]).
+        Returns (energy, f_all[nall,3], virial6 LAMMPS order, eatom[nlocal]) and, with
+        vatom=True, vatom[nlocal, 6] as a fifth element.
         """
         x = np.ascontiguousarray(x, dtype=np.float64)
         t = np.ascontiguousarray(lmp_type, dtype=np.int32)
@@ -210,27 +211,33 @@ class Potential:
         e = ctypes.c_double()
         vir = np.zeros(6)
         ea = np.zeros(max(nlocal, 1)) if eatom else None
+        va = np.zeros((max(nlocal, 1), 6)) if vatom else None
         _check(lib().mlipg_compute(self.h, nlocal, nall, _dp(x), _ip(t), len(il), _ip(il),
                                    _ip(nn), fp, 1, 1, _dp(f), ctypes.byref(e), _dp(vir),
-                                   _dp(ea) if eatom else None), self.h)
-        return e.value, f, vir, (ea[:nlocal] if eatom else None)
+                                   _dp(ea) if eatom else None, _dp(va) if vatom else None),
+               self.h)
+        out = (e.value, f, vir, (ea[:nlocal] if eatom else None))
+        return out + (va[:nlocal],) if vatom else out
 
-    def compute(self, system, eatom=True):
+    def compute(self, system, eatom=True, vatom=False):
         """Evaluates a `structures.System` through the LAMMPS-shaped C ABI."""
         off = system.nbr_off
         lists = [system.nbr_idx[off[i]:off[i + 1]] for i in range(system.nlocal)]
         nn = np.diff(off).astype(np.int32)
-        e, f, vir, ea = self.compute_lammps(system.nlocal, system.nall, system.x,
-                                            system.type + 1, np.arange(system.nlocal), nn, lists,
-                                            eatom)
-        return dict(energy=e, f_all=f, virial=vir, eatom=ea)
+        r = self.compute_lammps(system.nlocal, system.nall, system.x, system.type + 1,
+                                np.arange(system.nlocal), nn, lists, eatom, vatom)
+        out = dict(energy=r[0], f_all=r[1], virial=r[2], eatom=r[3])
+        if vatom:
+            out["vatom"] = r[4]
+        return out
 
     def compute_device(self, ncenters, x4, centers, nbr_off, nbr_idx, f, out8, eatom=None,
-                       img=None, cell=None, center_cell=None, fold=None, nb_cap=256):
+                       img=None, cell=None, center_cell=None, fold=None, nb_cap=256,
+                       vatom=None):
         """Stream-ordered call on device pointers (ints); see mlipg_compute_device."""
         _check(lib().mlipg_compute_device(self.h, ncenters, x4, centers, nbr_off, nbr_idx,
-                                          img, cell, center_cell, fold, nb_cap, f, eatom, out8),
-               self.h)
+                                          img, cell, center_cell, fold, nb_cap, f, eatom, vatom,
+                                          out8), self.h)
 
     def set_profiling(self, on: bool):
         _check(lib().mlipg_set_profiling(self.h, 1 if on else 0), self.h)
