@@ -631,10 +631,11 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
   if (lane == 0)
     for (int q = 0; q < 7; ++q) red[warp * 16 + q] = vals[q];
   __syncthreads();
-  if (tid < 7) {
+  if (tid < 8) {
     double s = 0;
-    for (int w = 0; w < kBlock / 32; ++w) s += red[w * 16 + tid];
-    A.partials[(size_t)blockIdx.x * 8 + tid] = s;
+    if (tid < 7)
+      for (int w = 0; w < kBlock / 32; ++w) s += red[w * 16 + tid];
+    A.partials[(size_t)blockIdx.x * 8 + tid] = s;   // slot 7 is a zeroed spare
   }
 }
 
