@@ -241,7 +241,10 @@ def run_ours(args, dist):
     nb_cap = int(np.diff(sysm.nbr_off).max())
     torch.cuda.synchronize()
 
-    def step(ncent=natoms):
+    ncent_main = min(natoms, args.centres) if args.centres > 0 else natoms
+
+    def step(ncent=None):
+        ncent = ncent_main if ncent is None else ncent
         with torch.cuda.stream(stream):
             d_f.zero_()
         g.compute_device(ncent, d_x4.data_ptr(), d_cent.data_ptr(), d_off.data_ptr(),
@@ -278,8 +281,15 @@ def run_ours(args, dist):
         t = torch.tensor([el_ms], dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         el_max = float(t.item())
-    value = natoms * args.steps * dist["world"] / (el_max * 1e-3)
+    value = ncent_main * args.steps * dist["world"] / (el_max * 1e-3)
     e_mixed = float(d_out[0].item())
+    if args.device_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "partial": True,
+                              "config": {"workload": args.workload, "centres": ncent_main},
+                              "kernel_ms_per_launch": ktimes, "clocks": clk}), flush=True)
+        g.close()
+        return
 
     # ---------------- e2e through the LAMMPS-shaped C ABI (host arrays)
     off = sysm.nbr_off
@@ -407,6 +417,10 @@ def main():
     ap.add_argument("--workload", default="fcc-ternary-1m", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--fp64-fraction", type=float, default=1.0 / 32)
+    ap.add_argument("--centres", type=int, default=0,
+                    help="evaluate only the first N centres per step (profiling runs)")
+    ap.add_argument("--device-only", action="store_true",
+                    help="time the device-resident step only (no e2e/FP64/accuracy/CPU legs)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
