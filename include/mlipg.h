@@ -113,6 +113,23 @@ int mlipg_compute_device(mlipg_handle* h, int ncenters, const void* d_x4, const 
                          int nb_cap, double* d_f, double* d_eatom, double* d_vatom,
                          double* d_out8);
 
+/* Allocation-free variant of mlipg_compute_device, for callers that cannot
+ * let the library call cudaMalloc (device memory owned by the caller's own
+ * pool or budget; latency-critical loops that must not enter the CUDA
+ * allocator).  Same arguments and outputs as mlipg_compute_device; the
+ * kernel's scratch (per-CTA partial sums and the status word) is a
+ * file-scope device array of 2048 CTA slots (128 KiB) that every GPU
+ * loading the library keeps until exit.  Launches needing more CTA slots
+ * fail with MLIPG_ECAPACITY.  All calls share that array: calls that overlap
+ * on the GPU race.  The first call on a device resolves the array's device
+ * address (cudaGetSymbolAddress); make it before any stream capture.
+ * No counterpart in the reference. */
+int mlipg_compute_device_noalloc(mlipg_handle* h, int ncenters, const void* d_x4,
+                                 const int* d_centers, const int* d_nbr_off,
+                                 const int* d_nbr_idx, const int* d_img, const double* d_cell,
+                                 const int* d_center_cell, const int* d_fold, int nb_cap,
+                                 double* d_f, double* d_eatom, double* d_vatom, double* d_out8);
+
 /* The handle's CUDA stream (cudaStream_t) for ordering caller work. */
 void* mlipg_stream(mlipg_handle* h);
 

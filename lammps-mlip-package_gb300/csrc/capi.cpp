@@ -600,3 +600,77 @@ extern "C" double mlipg_flops_per_atom_step(const mlipg_handle* h, int elem, dou
   return flops_per_atom_step(h->model, elem, nbar);
 }
 
+// Support of the allocation-free entry point (noalloc.cu): the same launch as
+// run_kernel, with the partial-sum and status scratch supplied by the caller
+// and without touching any grow-only buffer (nothing is allocated here).
+int mlipg_internal_fail(mlipg_handle* h, int code, const char* msg) {
+  return fail(h, code, "%s", msg);
+}
+
+int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x4,
+                                  const int* d_centers, const int* d_nbr_off,
+                                  const int* d_nbr_idx, const int* d_img, const double* d_cell,
+                                  const int* d_center_cell, const int* d_fold, int nb_cap,
+                                  double* d_f, double* d_eatom, double* d_vatom, double* d_out8,
+                                  double* partials, int partial_slots, int* status) {
+  if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
+  if (h->device < 0) return fail(h, MLIPG_ENOGPU, "no CUDA device is available");
+  if (ncenters < 0 || (ncenters > 0 && (!d_x4 || !d_centers || !d_nbr_off || !d_nbr_idx)) ||
+      !d_f || !d_out8)
+    return fail(h, MLIPG_EINVAL, "mlipg_compute_device_noalloc: invalid arguments");
+  if (d_img && (!d_cell || !d_center_cell))
+    return fail(h, MLIPG_EINVAL, "image codes need the cell lattices and centre cell ids");
+  const Model& M = h->model;
+  const bool fp64 = h->precision == MLIPG_PREC_FP64;
+  nb_cap = std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
+  const int nl_cap = std::max(M.max_nl, 1);
+  const size_t smem = fused_smem_bytes(fp64, M.T, M.Lh, nb_cap, nl_cap);
+  if (smem > 227 * 1024)
+    return fail(h, MLIPG_ENOTSUP, "model needs %zu bytes of shared memory per CTA", smem);
+  const int bps = fused_max_blocks_per_sm(fp64, M.L, smem);
+  if (bps < 1) return fail(h, MLIPG_ENOTSUP, "fused kernel cannot be resident (smem %zu)", smem);
+  const int grid = std::max(1, std::min(ncenters, bps * h->num_sms));
+  if (grid > partial_slots)
+    return fail(h, MLIPG_ECAPACITY,
+                "launch needs %d partial-sum slots; the no-allocation scratch holds %d", grid,
+                partial_slots);
+  CK(cudaMemsetAsync(status, 0, sizeof(int), h->stream), "memset status");
+  KernelArgs a{};
+  a.x4 = static_cast<const double4*>(d_x4);
+  a.centers = d_centers;
+  a.nbr_off = d_nbr_off;
+  a.nbr_idx = d_nbr_idx;
+  a.img = d_img;
+  a.cell = d_cell;
+  a.center_cell = d_center_cell;
+  a.fold = d_fold;
+  a.ncenters = ncenters;
+  a.terms = h->d_terms.as<DeviceTerm>();
+  a.units = h->d_units.as<DeviceUnit>();
+  a.unit_off = h->d_unit_off.as<int>();
+  a.nl_units = h->d_nl.as<DeviceUnit>();
+  a.nl_off = h->d_nl_off.as<int>();
+  a.poly = h->d_poly.as<DevicePoly>();
+  a.poly_off = h->d_poly_off.as<int>();
+  a.w_lin = h->d_wlin.as<double>();
+  a.radial = h->d_radial.as<double>();
+  a.T = M.T;
+  a.F = M.F;
+  a.L = M.L;
+  a.Lh = M.Lh;
+  a.nb_cap = nb_cap;
+  a.nl_cap = nl_cap;
+  a.rc = M.pot.cutoff;
+  a.f = d_f;
+  a.eatom = d_eatom;
+  a.vatom = d_vatom;
+  a.partials = partials;
+  a.status = status;
+  if (ncenters > 0) {
+    CK(launch_fused(fp64, M.L, a, grid, smem, h->stream), "fused kernel launch");
+  } else {
+    CK(cudaMemsetAsync(partials, 0, 8 * sizeof(double), h->stream), "memset partials");
+  }
+  CK(launch_finalize(partials, ncenters > 0 ? grid : 1, d_out8, h->stream), "finalize launch");
+  return MLIPG_OK;
+}

@@ -55,6 +55,8 @@ def lib():
         "mlipg_compute": (i32, [P, i32, i32, dp, ip, i32, ip, ip, ctypes.POINTER(ip), i32, i32,
                                 dp, dp, dp, dp, dp]),
         "mlipg_compute_device": (i32, [P, i32, P, P, P, P, P, P, P, P, i32, P, P, P, P]),
+        "mlipg_compute_device_noalloc": (i32, [P, i32, P, P, P, P, P, P, P, P, i32, P, P, P,
+                                               P]),
         "mlipg_stream": (P, [P]),
         "mlipg_device_status": (i32, [P, ip]),
         "mlipg_count_coefficients": (i32, [i32, i32, i32, i32, i32, ip, ip, i32, llp, llp]),
@@ -246,6 +248,14 @@ class Potential:
         buf = (ctypes.c_float * cap)()
         n = lib().mlipg_kernel_times(self.h, buf, cap)
         return [buf[k] for k in range(max(n, 0))]
+
+    def compute_device_noalloc(self, ncenters, x4, centers, nbr_off, nbr_idx, f, out8,
+                               eatom=None, img=None, cell=None, center_cell=None, fold=None,
+                               nb_cap=256, vatom=None):
+        """mlipg_compute_device_noalloc: same as compute_device, allocates nothing."""
+        _check(lib().mlipg_compute_device_noalloc(self.h, ncenters, x4, centers, nbr_off,
+                                                  nbr_idx, img, cell, center_cell, fold, nb_cap,
+                                                  f, eatom, vatom, out8), self.h)
 
     def device_status(self) -> int:
         b = ctypes.c_int()

@@ -49,6 +49,7 @@ def _sources():
         "neighbor.o": ("g++", os.path.join(CSRC, "neighbor.cpp")),
         "kernels_common.o": ("nvcc", os.path.join(CSRC, "kernels_common.cu")),
         "peak.o": ("nvcc", os.path.join(CSRC, "peak.cu")),
+        "noalloc.o": ("nvcc", os.path.join(CSRC, "noalloc.cu")),
         "kernels_f64.o": ("nvcc", os.path.join(CSRC, "kernels_f64.cu")),
         "kernels_f32.o": ("nvcc", os.path.join(CSRC, "kernels_f32.cu")),
     }
