@@ -276,6 +276,9 @@ def run_ours(args, dist):
     g.set_profiling(False)
     el_ms = ev0.elapsed_time(ev1)
     ktimes = g.kernel_times()
+    phases = g.phase_cycles()
+    ptot = max(sum(phases.values()), 1)
+    phase_share = {k: round(v / ptot, 4) for k, v in phases.items()}
     el_max = el_ms
     if dist["world"] > 1:
         t = torch.tensor([el_ms], dtype=torch.float64)
@@ -287,7 +290,8 @@ def run_ours(args, dist):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "partial": True,
                               "config": {"workload": args.workload, "centres": ncent_main},
-                              "kernel_ms_per_launch": ktimes, "clocks": clk}), flush=True)
+                              "kernel_ms_per_launch": ktimes, "phase_share": phase_share,
+                              "clocks": clk}), flush=True)
         g.close()
         return
 
@@ -403,7 +407,7 @@ def run_ours(args, dist):
                 "energy_eV": e_mixed,
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": 2 * args.steps,
-                "kernel_ms_per_launch": kt}
+                "kernel_ms_per_launch": kt, "phase_share": phase_share}
         print(json.dumps(line), flush=True)
     g.close()
 

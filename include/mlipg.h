@@ -162,11 +162,51 @@ double mlipg_flops_per_atom_step(const mlipg_handle* h, int elem, double nbar);
  * Returns the number copied.  Measurement support; no reference counterpart. */
 int mlipg_set_profiling(mlipg_handle* h, int on);
 int mlipg_kernel_times(mlipg_handle* h, float* ms, int cap);
+/* With profiling on, SM cycles (summed over CTAs, thread-0 view) the fused
+ * kernel spent in its phases since the last call: [0] neighbour compaction,
+ * [1] order parameters, [2] nonlinear features + polynomial, [3] invariants
+ * and adjoint, [4] forces and reductions. */
+int mlipg_phase_cycles(mlipg_handle* h, unsigned long long* out8);
 
 /* Live FMA throughput of the CUDA-core FP32 (fp64 = 0) or FP64 (fp64 = 1)
  * pipe on the current device, in TFLOP/s: the roofline denominator of the
  * fused kernel.  Measurement support; no reference counterpart. */
 int mlipg_measure_fma_peak(int fp64, double* tflops);
+
+/* Many independent periodic cells (uneven atom counts) evaluated in one
+ * persistent launch.  mlipg_batch_create wraps each cell's atoms into its cell
+ * (lattices: 9 doubles per cell, rows a1 a2 a3), builds image-coded full
+ * lists (no ghost atoms; small cells see their own images) and uploads
+ * everything once.  mlipg_batch_compute evaluates all cells: energies[ncells]
+ * (eV), forces[natoms_total*3] (eV/A) and virials[ncells*6] (LAMMPS order)
+ * back on the host; mlipg_batch_launch only enqueues the evaluation on the
+ * handle's stream.  No counterpart in the reference (one structure per
+ * MLIPModel::set_structure call, mlipkk.cpp:278-372). */
+typedef struct mlipg_batch mlipg_batch;
+int mlipg_batch_create(mlipg_handle* h, int ncells, const int* natoms, const double* lattices,
+                       const double* x, const int* elements, mlipg_batch** out);
+int mlipg_batch_launch(mlipg_batch* b);
+int mlipg_batch_compute(mlipg_batch* b, double* energies, double* forces, double* virials);
+int mlipg_batch_sizes(const mlipg_batch* b, int* natoms, long long* npairs);
+void mlipg_batch_destroy(mlipg_batch* b);
+
+/* NVE molecular dynamics on the device (velocity Verlet as LAMMPS `fix nve`,
+ * metal units: A, ps, eV, g/mol; masses from the potential file).  Positions
+ * x[natoms*3] and optional velocities v (A/ps) of one periodic cell
+ * (lattice9 rows a1 a2 a3), elements 0-based; the full list is built with
+ * cutoff + skin and rebuilt when an atom moves more than skin/2.  Each step
+ * runs as one CUDA graph launch when use_graph is non-zero.  Reproduces the
+ * trajectories of the reference's regression runs (fix nve,
+ * test/regression/*.in); LAMMPS itself owns integration in the drop-in path.
+ * mlipg_md_thermo: [pe, ke, T (K), etotal, P, Pxx Pyy Pzz Pxy Pxz Pyz (bar),
+ * list rebuilds], with dof = 3N - 3 as LAMMPS's thermo_temp. */
+typedef struct mlipg_md mlipg_md;
+int mlipg_md_create(mlipg_handle* h, const double* lattice9, int natoms, const double* x,
+                    const double* v, const int* elements, double skin, mlipg_md** out);
+int mlipg_md_run(mlipg_md* md, int nsteps, double dt_ps, int use_graph);
+int mlipg_md_state(mlipg_md* md, double* x, double* v, double* f);
+int mlipg_md_thermo(mlipg_md* md, double* out12);
+void mlipg_md_destroy(mlipg_md* md);
 
 /* Host neighbour-list builder for standalone and batched use: owned atoms
  * (wrapped into the cell), ghost images within `cutoff` in fractional

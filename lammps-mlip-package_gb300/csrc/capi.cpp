@@ -83,6 +83,7 @@ struct mlipg_handle {
   cudaStream_t stream = nullptr;
   // model tables on the device
   DevBuf d_terms, d_units, d_unit_off, d_nl, d_nl_off, d_poly, d_poly_off, d_wlin, d_radial;
+  DevBuf d_iunits, d_iunit_off, d_tuples, d_wlin_f, d_phase;
   // per-call buffers (grow only)
   DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_vatom, d_partials, d_status, d_out8;
   HostBuf h_x4, h_centers, h_off, h_idx, h_f, h_eatom, h_out;
@@ -126,9 +127,18 @@ static int upload_model(mlipg_handle* h) {
   const Model& M = h->model;
   std::vector<DeviceUnit> units, nl;
   std::vector<DevicePoly> poly;
-  std::vector<int> uoff(M.T + 1, 0), noff(M.T + 1, 0), poff(M.T + 1, 0);
+  std::vector<DeviceIrrUnit> iunits;
+  std::vector<DeviceTuple> tuples;
+  std::vector<int> uoff(M.T + 1, 0), noff(M.T + 1, 0), poff(M.T + 1, 0), ioff(M.T + 1, 0);
   for (int t = 0; t < M.T; ++t) {
     const Schedule& S = M.sched[t];
+    ioff[t] = (int)iunits.size();
+    const int tbase = (int)tuples.size();
+    for (DeviceIrrUnit iu : S.iunits) {
+      iu.tup += tbase;
+      iunits.push_back(iu);
+    }
+    tuples.insert(tuples.end(), S.tuples.begin(), S.tuples.end());
     uoff[t] = (int)units.size();
     noff[t] = (int)nl.size();
     poff[t] = (int)poly.size();
@@ -136,6 +146,7 @@ static int upload_model(mlipg_handle* h) {
     nl.insert(nl.end(), S.nl_units.begin(), S.nl_units.end());
     poly.insert(poly.end(), S.poly.begin(), S.poly.end());
   }
+  ioff[M.T] = (int)iunits.size();
   uoff[M.T] = (int)units.size();
   noff[M.T] = (int)nl.size();
   poff[M.T] = (int)poly.size();
@@ -147,12 +158,19 @@ static int upload_model(mlipg_handle* h) {
   cudaStream_t s = h->stream;
   CK(upload(h->d_terms, M.cterms, s), "upload terms");
   CK(upload(h->d_units, units, s), "upload units");
+  CK(upload(h->d_iunits, iunits, s), "upload batched units");
+  CK(upload(h->d_iunit_off, ioff, s), "upload batched unit offsets");
+  CK(upload(h->d_tuples, tuples, s), "upload tuples");
   CK(upload(h->d_unit_off, uoff, s), "upload unit offsets");
   CK(upload(h->d_nl, nl, s), "upload nonlinear units");
   CK(upload(h->d_nl_off, noff, s), "upload nonlinear offsets");
   CK(upload(h->d_poly, poly, s), "upload polynomial");
   CK(upload(h->d_poly_off, poff, s), "upload polynomial offsets");
   CK(upload(h->d_wlin, M.w_lin, s), "upload linear weights");
+  {
+    std::vector<float> wf(M.w_lin.begin(), M.w_lin.end());
+    CK(upload(h->d_wlin_f, wf, s), "upload linear weights (FP32)");
+  }
   CK(upload(h->d_radial, radial, s), "upload radial parameters");
   CK(cudaStreamSynchronize(s), "model upload");
   return MLIPG_OK;
@@ -221,7 +239,8 @@ int mlipg_destroy(mlipg_handle* h) {
     delete h;
     return MLIPG_OK;
   }
-  DevBuf* bufs[] = {&h->d_terms, &h->d_units, &h->d_unit_off, &h->d_nl, &h->d_nl_off,
+  DevBuf* bufs[] = {&h->d_iunits, &h->d_iunit_off, &h->d_tuples, &h->d_wlin_f, &h->d_phase,
+                    &h->d_terms, &h->d_units, &h->d_unit_off, &h->d_nl, &h->d_nl_off,
                     &h->d_poly, &h->d_poly_off, &h->d_wlin, &h->d_radial, &h->d_x4,
                     &h->d_centers, &h->d_off, &h->d_idx, &h->d_f, &h->d_eatom, &h->d_vatom, &h->d_partials,
                     &h->d_status, &h->d_out8};
@@ -325,11 +344,16 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.terms = h->d_terms.as<DeviceTerm>();
   a.units = h->d_units.as<DeviceUnit>();
   a.unit_off = h->d_unit_off.as<int>();
+  a.iunits = h->d_iunits.as<DeviceIrrUnit>();
+  a.iunit_off = h->d_iunit_off.as<int>();
+  a.tuples = h->d_tuples.as<DeviceTuple>();
   a.nl_units = h->d_nl.as<DeviceUnit>();
   a.nl_off = h->d_nl_off.as<int>();
   a.poly = h->d_poly.as<DevicePoly>();
   a.poly_off = h->d_poly_off.as<int>();
   a.w_lin = h->d_wlin.as<double>();
+  a.w_lin_f = h->d_wlin_f.as<float>();
+  a.phase_clocks = h->profiling ? h->d_phase.as<unsigned long long>() : nullptr;
   a.radial = h->d_radial.as<double>();
   a.T = M.T;
   a.F = M.F;
@@ -522,7 +546,22 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
 
 extern "C" int mlipg_set_profiling(mlipg_handle* h, int on) {
   if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
+  if (on && h->device >= 0) {
+    CK(h->d_phase.reserve(8 * sizeof(unsigned long long)), "alloc phase clocks");
+    CK(cudaMemset(h->d_phase.p, 0, 8 * sizeof(unsigned long long)), "memset phase clocks");
+  }
   h->profiling = on != 0;
+  return MLIPG_OK;
+}
+
+extern "C" int mlipg_phase_cycles(mlipg_handle* h, unsigned long long* out8) {
+  if (!h || !out8) return fail(h, MLIPG_EINVAL, "null argument");
+  for (int k = 0; k < 8; ++k) out8[k] = 0;
+  if (h->device < 0 || !h->d_phase.p) return MLIPG_OK;
+  CK(cudaStreamSynchronize(h->stream), "phase clocks");
+  CK(cudaMemcpy(out8, h->d_phase.p, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost),
+     "copy phase clocks");
+  CK(cudaMemset(h->d_phase.p, 0, 8 * sizeof(unsigned long long)), "reset phase clocks");
   return MLIPG_OK;
 }
 
@@ -600,6 +639,7 @@ extern "C" double mlipg_flops_per_atom_step(const mlipg_handle* h, int elem, dou
   return flops_per_atom_step(h->model, elem, nbar);
 }
 
+
 // Support of the allocation-free entry point (noalloc.cu): the same launch as
 // run_kernel, with the partial-sum and status scratch supplied by the caller
 // and without touching any grow-only buffer (nothing is allocated here).
@@ -648,11 +688,16 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
   a.terms = h->d_terms.as<DeviceTerm>();
   a.units = h->d_units.as<DeviceUnit>();
   a.unit_off = h->d_unit_off.as<int>();
+  a.iunits = h->d_iunits.as<DeviceIrrUnit>();
+  a.iunit_off = h->d_iunit_off.as<int>();
+  a.tuples = h->d_tuples.as<DeviceTuple>();
   a.nl_units = h->d_nl.as<DeviceUnit>();
   a.nl_off = h->d_nl_off.as<int>();
   a.poly = h->d_poly.as<DevicePoly>();
   a.poly_off = h->d_poly_off.as<int>();
   a.w_lin = h->d_wlin.as<double>();
+  a.w_lin_f = h->d_wlin_f.as<float>();
+  a.phase_clocks = h->profiling ? h->d_phase.as<unsigned long long>() : nullptr;
   a.radial = h->d_radial.as<double>();
   a.T = M.T;
   a.F = M.F;

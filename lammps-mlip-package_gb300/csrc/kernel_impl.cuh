@@ -4,8 +4,9 @@
 // over centres); every intermediate of the reference's seven stages stays in
 // shared memory:
 //   P1  neighbour compaction: keep r <= rc, stable-sort by element (warp 0)
-//   P2  order parameters a[s][lm][n] = sum_j f_n(r) conj(Y_lm), products in
-//       REAL, sums in FP64 (mlipkk_lmp.h:314-387, mlipkk_features_kk.h:9-48,
+//   P2  order parameters a[s][lm][n] = sum_j f_n(r) conj(Y_lm): f_n and Y_lm
+//       evaluated in REAL, staged as FP64 and summed with FP64 FMAs
+//       (mlipkk_lmp.h:314-387, mlipkk_features_kk.h:9-48,
 //       mlipkk_spherical_harmonics_kk.h:18-81)
 //   P3  nonlinear features and polynomial terms of order >= 2: energy part
 //       and H = dE/dd for those features (mlipkk_lmp.h:489-625)
@@ -37,6 +38,10 @@ template <typename T> struct Cx;
 template <> struct Cx<float> { using type = float2; };
 template <> struct Cx<double> { using type = double2; };
 using Rc = Cx<R>::type;
+// resident CTAs per SM the register allocation targets: two for FP32
+// products (shared memory allows two), one for FP64 (its shared memory
+// allows only one, so registers are not capped)
+constexpr int kMinBlocks = sizeof(R) == 4 ? 2 : 1;
 
 namespace {
 
@@ -182,19 +187,44 @@ __device__ __forceinline__ void radial(const double* __restrict__ prm, int F, R 
   }
 }
 
+// Stages Y_lm of one neighbour as FP64 (exact conversion of the REAL value)
+// for the FP64 order-parameter sums.
+// radial basis for the 4 channels n0..n0+3 (P6: 4 threads per neighbour)
+__device__ __forceinline__ void radial4(const double* __restrict__ prm, int F, int n0, R r, R rc,
+                                        R* f, R* fd) {
+  R sn, cs;
+  sincospi_r(r / rc, &sn, &cs);
+  const bool in = r < rc;
+  const R fc = in ? R(0.5) * (cs + R(1)) : R(0);
+  const R fcd = in ? R(-0.5) * R(3.14159265358979323846) / rc * sn : R(0);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int n = n0 + q;
+    if (n < F) {
+      const R beta = (R)__ldg(prm + 2 * n), mu = (R)__ldg(prm + 2 * n + 1);
+      const R dr = r - mu;
+      const R bf = exp_r(-beta * dr * dr);
+      f[q] = bf * fc;
+      fd[q] = (R(-2) * beta * dr * bf) * fc + bf * fcd;
+    } else {
+      f[q] = R(0);
+      fd[q] = R(0);
+    }
+  }
+}
+
 struct StageVis {
-  Rc* ys;
+  double2* ys;
   int slot;
   __device__ __forceinline__ void operator()(int lmh, int, R yre, R yim, R, R, R, R, R, R) {
-    ys[lmh * kChunk + slot] = Rc{yre, yim};
+    ys[lmh * kChunk + slot] = double2{(double)yre, (double)yim};
   }
 };
 
 struct ForceVis {
-  const Rc* g;   // G of the neighbour's element slot: [Lh][16]
-  const R* f;
+  const Rc* g;   // G of the neighbour's element slot, offset to channel n0: [Lh][16]
+  const R* f;    // f_n, f'_n of channels n0..n0+3
   const R* fd;
-  int F;
   R ux, uy, uz;
   R fx, fy, fz;
   __device__ __forceinline__ void operator()(int lmh, int mp, R yre, R yim, R xre, R xim, R yyre,
@@ -202,14 +232,12 @@ struct ForceVis {
     const Rc* gg = g + lmh * kNPad;
     R g0r = 0, g0i = 0, g1r = 0, g1i = 0;
 #pragma unroll
-    for (int n = 0; n < kNPad; ++n) {
-      if (n < F) {
-        const Rc v = gg[n];
-        g0r += f[n] * v.x;
-        g0i += f[n] * v.y;
-        g1r += fd[n] * v.x;
-        g1i += fd[n] * v.y;
-      }
+    for (int q = 0; q < 4; ++q) {
+      const Rc v = gg[q];
+      g0r += f[q] * v.x;
+      g0i += f[q] * v.y;
+      g1r += fd[q] * v.x;
+      g1i += fd[q] * v.y;
     }
     const R coeff = (mp == 0) ? R(1) : R(2);
     const R ry = yre * g1r + yim * g1i;
@@ -316,6 +344,183 @@ __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* 
   }
 }
 
+// linear weights in the arithmetic precision of the products
+__device__ __forceinline__ const float* wlin_pick(const double*, const float* f, float*) { return f; }
+__device__ __forceinline__ const double* wlin_pick(const double* d, const float*, double*) { return d; }
+__device__ __forceinline__ const R* wlin_table(const KernelArgs& A) {
+  return wlin_pick(A.w_lin, A.w_lin_f, (R*)nullptr);
+}
+
+// Element tuples of one irreps (order Q <= 3, TT elements) over a chunk of
+// canonical terms.  For Q = 3 and TT = 3 a unit fixes the first slot's
+// element (u.s0) and covers the TT*TT tuples of the other two slots, which
+// keeps the unit's registers low enough for two resident CTAs per SM.  Per
+// term: order-parameter loads shared by all tuples, shared leave-one-out
+// products, per-tuple invariant sums d[j] (REAL) and adjoint partials per
+// (slot, element) in registers, flushed once per term.
+template <int Q, int TT, bool FIX0>
+__device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
+                                        const DeviceTerm* __restrict__ terms,
+                                        const R* __restrict__ wlin, const double* hnl,
+                                        const Rc* sa, Rc* sg, int Lh, int n, int half, bool act,
+                                        double& eacc) {
+  constexpr int N0 = FIX0 ? 1 : TT;                       // elements of slot 0 in this unit
+  constexpr int NT = (Q == 1) ? N0 : (Q == 2 ? N0 * TT : N0 * TT * TT);
+  const int s0base = FIX0 ? (int)u.s0 : 0;
+  R H[NT], d[NT];
+#pragma unroll
+  for (int j = 0; j < NT; ++j) {
+    const int2 e = __ldg(reinterpret_cast<const int2*>(tups + u.tup + j));
+    R h = R(0);
+    if (act && e.x >= 0) {
+      h = __ldg(wlin + (size_t)e.x * kNPad + n);
+      if (e.y >= 0) h = (R)((double)h + hnl[e.y * kNPad + n]);
+    }
+    H[j] = h;
+    d[j] = R(0);
+  }
+  const int es = Lh * kNPad;   // element stride in the a / G arrays
+  const int kend = u.term0 + u.nterm;
+  for (int k = u.term0 + half; k < kend; k += 2) {
+    const int4 raw = __ldg(reinterpret_cast<const int4*>(terms + k));
+    const R c = (R)__hiloint2double(raw.y, raw.x);
+    const unsigned lw = (unsigned)raw.z, code = ((unsigned)raw.w) >> 16;
+    const bool self = (code >> 12) & 1u;
+    const R ce = self ? c : R(2) * c;
+    int lo[Q];
+    R ar0[N0], ai0[N0];
+    R ar[Q][TT], ai[Q][TT];    // slots >= 1 (slot 0 uses ar0 / ai0)
+#pragma unroll
+    for (int p = 0; p < Q; ++p) {
+      lo[p] = (int)((lw >> (8 * p)) & 255u) * kNPad + n;
+      const bool cj = ((code >> (2 * p)) & 3u) == (unsigned)kSlotConj;
+      if (p == 0) {
+#pragma unroll
+        for (int s = 0; s < N0; ++s) {
+          const Rc v = sa[(s0base + s) * es + lo[0]];
+          ar0[s] = v.x;
+          ai0[s] = cj ? -v.y : v.y;
+        }
+      } else {
+#pragma unroll
+        for (int s = 0; s < TT; ++s) {
+          const Rc v = sa[s * es + lo[p]];
+          ar[p][s] = v.x;
+          ai[p][s] = cj ? -v.y : v.y;
+        }
+      }
+    }
+    R g0r[N0], g0i[N0], gr[Q][TT], gi[Q][TT];
+#pragma unroll
+    for (int s = 0; s < N0; ++s) { g0r[s] = R(0); g0i[s] = R(0); }
+#pragma unroll
+    for (int p = 0; p < Q; ++p)
+#pragma unroll
+      for (int s = 0; s < TT; ++s) { gr[p][s] = R(0); gi[p][s] = R(0); }
+    if (Q == 1) {
+#pragma unroll
+      for (int s0 = 0; s0 < N0; ++s0) {
+        d[s0] += ce * ar0[s0];
+        g0r[s0] += H[s0];
+      }
+    } else if (Q == 2) {
+#pragma unroll
+      for (int s0 = 0; s0 < N0; ++s0)
+#pragma unroll
+        for (int s1 = 0; s1 < TT; ++s1) {
+          const int j = s0 * TT + s1;
+          d[j] += ce * (ar0[s0] * ar[1][s1] - ai0[s0] * ai[1][s1]);
+          const R h = H[j];
+          g0r[s0] += h * ar[1][s1]; g0i[s0] += h * ai[1][s1];
+          gr[1][s1] += h * ar0[s0]; gi[1][s1] += h * ai0[s0];
+        }
+    } else {
+      // b12[s1][s2] = a1 a2 (adjoint of slot 0)
+      R b12r[TT][TT], b12i[TT][TT];
+#pragma unroll
+      for (int x = 0; x < TT; ++x)
+#pragma unroll
+        for (int y = 0; y < TT; ++y) {
+          b12r[x][y] = ar[1][x] * ar[2][y] - ai[1][x] * ai[2][y];
+          b12i[x][y] = ar[1][x] * ai[2][y] + ai[1][x] * ar[2][y];
+        }
+#pragma unroll
+      for (int s0 = 0; s0 < N0; ++s0) {
+        R b02r[TT], b02i[TT];   // a0 a2 (adjoint of slot 1)
+#pragma unroll
+        for (int y = 0; y < TT; ++y) {
+          b02r[y] = ar0[s0] * ar[2][y] - ai0[s0] * ai[2][y];
+          b02i[y] = ar0[s0] * ai[2][y] + ai0[s0] * ar[2][y];
+        }
+#pragma unroll
+        for (int s1 = 0; s1 < TT; ++s1) {
+          const R pr = ar0[s0] * ar[1][s1] - ai0[s0] * ai[1][s1];   // a0 a1 (slot 2)
+          const R pi = ar0[s0] * ai[1][s1] + ai0[s0] * ar[1][s1];
+#pragma unroll
+          for (int s2 = 0; s2 < TT; ++s2) {
+            const int j = (s0 * TT + s1) * TT + s2;
+            d[j] += ce * (pr * ar[2][s2] - pi * ai[2][s2]);
+            const R h = H[j];
+            g0r[s0] += h * b12r[s1][s2]; g0i[s0] += h * b12i[s1][s2];
+            gr[1][s1] += h * b02r[s2];   gi[1][s1] += h * b02i[s2];
+            gr[2][s2] += h * pr;         gi[2][s2] += h * pi;
+          }
+        }
+      }
+    }
+    if (act) {
+#pragma unroll
+      for (int p = 0; p < Q; ++p) {
+        const unsigned cd = (code >> (2 * p)) & 3u;
+        const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
+        const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
+        if (p == 0) {
+#pragma unroll
+          for (int s = 0; s < N0; ++s) {
+            Rc* gp = sg + (s0base + s) * es + lo[0];
+            atomicAdd(&gp->x, kr * g0r[s]);
+            if (cd < 2u) atomicAdd(&gp->y, ki * g0i[s]);
+          }
+        } else {
+#pragma unroll
+          for (int s = 0; s < TT; ++s) {
+            Rc* gp = sg + s * es + lo[p];
+            atomicAdd(&gp->x, kr * gr[p][s]);
+            if (cd < 2u) atomicAdd(&gp->y, ki * gi[p][s]);
+          }
+        }
+      }
+    }
+  }
+  // combine the two half-warps' term sums; sum_j w_j d_j for this unit in
+  // REAL, accumulated into the centre's FP64 energy
+  R eu = R(0);
+#pragma unroll
+  for (int j = 0; j < NT; ++j) {
+    const R dj = d[j] + __shfl_xor_sync(0xffffffffu, d[j], 16);
+    const int itc = __ldg(reinterpret_cast<const int*>(tups + u.tup + j));
+    if (itc >= 0 && act) eu += __ldg(wlin + (size_t)itc * kNPad + n) * dj;
+  }
+  if (half == 0 && act) eacc += (double)eu;
+}
+
+template <int TT>
+__device__ __forceinline__ void dispatch_irr(const DeviceIrrUnit& u, const DeviceTuple* tups,
+                                             const DeviceTerm* terms, const R* wlin,
+                                             const double* hnl, const Rc* sa, Rc* sg, int Lh,
+                                             int n, int half, bool act, double& eacc) {
+  switch (u.q) {
+    case 1: run_irr<1, TT, false>(u, tups, terms, wlin, hnl, sa, sg, Lh, n, half, act, eacc); break;
+    case 2: run_irr<2, TT, false>(u, tups, terms, wlin, hnl, sa, sg, Lh, n, half, act, eacc); break;
+    default:
+      if (TT == 3)
+        run_irr<3, TT, true>(u, tups, terms, wlin, hnl, sa, sg, Lh, n, half, act, eacc);
+      else
+        run_irr<3, TT, false>(u, tups, terms, wlin, hnl, sa, sg, Lh, n, half, act, eacc);
+      break;
+  }
+}
+
 template <bool WITH_G>
 __device__ __forceinline__ void dispatch_unit(const DeviceUnit& u, const DeviceTerm* terms,
                                               const Rc* sa, Rc* sg, int Lh, int n, int half,
@@ -341,7 +546,7 @@ struct SmemLayout {
 __host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int nl_cap) {
   SmemLayout s;
   const size_t an = (size_t)T * Lh * kNPad * sizeof(Rc);
-  const size_t stage = (size_t)Lh * kChunk * sizeof(Rc) + (size_t)kChunk * kNPad * sizeof(R);
+  const size_t stage = (size_t)Lh * kChunk * sizeof(double2) + (size_t)kChunk * kNPad * sizeof(double);
   s.a = 0;
   s.g = align16(an);
   s.dnl = s.g + align16(an > stage ? an : stage);
@@ -354,14 +559,14 @@ __host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int
 }
 
 template <int LCAP>
-__global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ KernelArgs A) {
+__global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_constant__ KernelArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int T = A.T, F = A.F, Lh = A.Lh, L = A.L;
   const SmemLayout lay = smem_layout(T, Lh, A.nb_cap, A.nl_cap);
   Rc* sa = reinterpret_cast<Rc*>(smem + lay.a);
   Rc* sg = reinterpret_cast<Rc*>(smem + lay.g);
-  Rc* ys = sg;                                                      // P2 staging
-  R* fs = reinterpret_cast<R*>(smem + lay.g + (size_t)Lh * kChunk * sizeof(Rc));
+  double2* ys = reinterpret_cast<double2*>(sg);                     // P2 staging (FP64)
+  double* fs = reinterpret_cast<double*>(smem + lay.g + (size_t)Lh * kChunk * sizeof(double2));
   double* dnl = reinterpret_cast<double*>(smem + lay.dnl);
   double* hnl = reinterpret_cast<double*>(smem + lay.hnl);
   int* nbk = reinterpret_cast<int*>(smem + lay.nbk);
@@ -375,6 +580,15 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
 
   double vir[6] = {0, 0, 0, 0, 0, 0};
   double ecta = 0.0;
+  unsigned long long ph[6] = {0, 0, 0, 0, 0, 0};   // thread 0: cycles per phase
+  long long tstamp = 0;
+  const bool prof = A.phase_clocks != nullptr;
+#define MLIPG_STAMP(k)                          \
+  if (prof && tid == 0) {                       \
+    const long long t_ = clock64();             \
+    ph[k] += (unsigned long long)(t_ - tstamp); \
+    tstamp = t_;                                \
+  }
 
   for (int c = blockIdx.x; c < A.ncenters; c += gridDim.x) {
     const int i = __ldg(A.centers + c);
@@ -388,6 +602,7 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
       continue;
     }
     const int o0 = __ldg(A.nbr_off + c), o1 = __ldg(A.nbr_off + c + 1);
+    if (prof && tid == 0) tstamp = clock64();
     // ---------------------------------------------------------------- P1
     if (warp == 0) {
       int cnt[kMaxTypes];
@@ -459,6 +674,7 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
       continue;
     }
     const int nkeep = misc[T];
+    MLIPG_STAMP(0)
     // ---------------------------------------------------------------- P2
     for (int t = 0; t < T; ++t) {
       double accr[kEPT], acci[kEPT];
@@ -476,7 +692,7 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
           R f[kNPad], fdum[kNPad];
           radial(A.radial, F, (R)r, rc, f, fdum, false);
 #pragma unroll
-          for (int n = 0; n < kNPad; ++n) fs[tid * kNPad + n] = f[n];
+          for (int n = 0; n < kNPad; ++n) fs[tid * kNPad + n] = (double)f[n];
           StageVis v{ys, tid};
           sh_visit<LCAP, false>((R)dx, (R)dy, (R)dz, (R)r, L, v);
         }
@@ -487,10 +703,10 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
           const int lmh = idx >> 4, n = idx & 15;
           if (lmh < Lh && n < F) {
             for (int jj = 0; jj < csz; ++jj) {
-              const R fv = fs[jj * kNPad + n];
-              const Rc y = ys[lmh * kChunk + jj];
-              accr[e] += (double)(fv * y.x);
-              acci[e] -= (double)(fv * y.y);
+              const double fv = fs[jj * kNPad + n];
+              const double2 y = ys[lmh * kChunk + jj];
+              accr[e] = fma(fv, y.x, accr[e]);
+              acci[e] = fma(-fv, y.y, acci[e]);
             }
           }
         }
@@ -503,6 +719,7 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
         if (lmh < Lh) sa[(t * Lh + lmh) * kNPad + (idx & 15)] = Rc{(R)accr[e], (R)acci[e]};
       }
     }
+    MLIPG_STAMP(1)
     // ---------------------------------------------------------------- P3
     double eacc = 0.0;
     const int nl0 = __ldg(A.nl_off + ti), nNL = __ldg(A.nl_off + ti + 1) - nl0;
@@ -545,11 +762,23 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
     // ---------------------------------------------------------------- P4
     for (int e = tid; e < T * Lh * kNPad; e += kBlock) sg[e] = Rc{R(0), R(0)};
     __syncthreads();
+    MLIPG_STAMP(2)
     // ---------------------------------------------------------------- P5
     {
       const int u0 = __ldg(A.unit_off + ti), nU = __ldg(A.unit_off + ti + 1) - u0;
+      const int i0 = __ldg(A.iunit_off + ti), nI = __ldg(A.iunit_off + ti + 1) - i0;
       // static round-robin over warps (units are sorted by cost): each
       // thread's energy sum has a fixed order, so energies are reproducible
+      const R* wl = wlin_table(A);
+      for (int u = warp; u < nI; u += kBlock / 32) {
+        const DeviceIrrUnit iu = A.iunits[i0 + u];
+        if (T == 3)
+          dispatch_irr<3>(iu, A.tuples, A.terms, wl, hnl, sa, sg, Lh, n, half, act, eacc);
+        else if (T == 2)
+          dispatch_irr<2>(iu, A.tuples, A.terms, wl, hnl, sa, sg, Lh, n, half, act, eacc);
+        else
+          dispatch_irr<1>(iu, A.tuples, A.terms, wl, hnl, sa, sg, Lh, n, half, act, eacc);
+      }
       for (int u = warp; u < nU; u += kBlock / 32) {
         const DeviceUnit un = A.units[u0 + u];
         double hv = 0.0;
@@ -564,32 +793,49 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
       }
     }
     __syncthreads();
+    MLIPG_STAMP(3)
     // ---------------------------------------------------------------- P6
     double fix = 0.0, fiy = 0.0, fiz = 0.0;
     double va[6] = {0, 0, 0, 0, 0, 0};   // this centre's virial (reference order)
-    for (int jj = tid; jj < nkeep; jj += kBlock) {
-      const int k = nbk[jj];
-      const int j = __ldg(A.nbr_idx + k);
-      const double4 xj = A.x4[j];
-      const int tj = (int)xj.w;
-      double dx, dy, dz;
-      pair_disp(A, c, k, xi, xj, dx, dy, dz);
-      const double r = sqrt(dx * dx + dy * dy + dz * dz);
-      R f[kNPad], fd[kNPad];
-      radial(A.radial, F, (R)r, rc, f, fd, true);
-      const double ir = 1.0 / r;
-      ForceVis v{sg + (size_t)tj * Lh * kNPad, f, fd, F, (R)(dx * ir), (R)(dy * ir), (R)(dz * ir),
-                 R(0), R(0), R(0)};
-      sh_visit<LCAP, true>((R)dx, (R)dy, (R)dz, (R)r, L, v);
-      const double fx = v.fx, fy = v.fy, fz = v.fz;
-      fix += fx; fiy += fy; fiz += fz;
-      const int fj = A.fold ? __ldg(A.fold + j) : j;
-      atomicAdd(A.f + 3 * (size_t)fj, -fx);
-      atomicAdd(A.f + 3 * (size_t)fj + 1, -fy);
-      atomicAdd(A.f + 3 * (size_t)fj + 2, -fz);
-      // reference component order: xx yy zz yz zx xy
-      va[0] -= dx * fx; va[1] -= dy * fy; va[2] -= dz * fz;
-      va[3] -= dy * fz; va[4] -= dz * fx; va[5] -= dx * fy;
+    {
+      // 4 threads per neighbour; thread `sub` owns radial channels 4*sub..4*sub+3
+      const int sub = tid & 3, n0 = 4 * sub;
+      const int rounds = (nkeep + kBlock / 4 - 1) / (kBlock / 4);
+      for (int it = 0; it < rounds; ++it) {
+        const int jj = it * (kBlock / 4) + (tid >> 2);
+        const bool valid = jj < nkeep;
+        const int k = valid ? nbk[jj] : nbk[0];
+        const int j = __ldg(A.nbr_idx + k);
+        const double4 xj = A.x4[j];
+        const int tj = valid ? (int)xj.w : 0;
+        double dx, dy, dz;
+        pair_disp(A, c, k, xi, xj, dx, dy, dz);
+        if (!valid) { dx = 1.0; dy = 0.0; dz = 0.0; }
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        R f[4], fd[4];
+        radial4(A.radial, F, n0, (R)r, rc, f, fd);
+        const double ir = 1.0 / r;
+        ForceVis v{sg + (size_t)tj * Lh * kNPad + n0, f, fd, (R)(dx * ir), (R)(dy * ir),
+                   (R)(dz * ir), R(0), R(0), R(0)};
+        sh_visit<LCAP, true>((R)dx, (R)dy, (R)dz, (R)r, L, v);
+        double fx = v.fx, fy = v.fy, fz = v.fz;
+        fx += __shfl_xor_sync(0xffffffffu, fx, 1);
+        fy += __shfl_xor_sync(0xffffffffu, fy, 1);
+        fz += __shfl_xor_sync(0xffffffffu, fz, 1);
+        fx += __shfl_xor_sync(0xffffffffu, fx, 2);
+        fy += __shfl_xor_sync(0xffffffffu, fy, 2);
+        fz += __shfl_xor_sync(0xffffffffu, fz, 2);
+        if (valid && sub == 0) {
+          fix += fx; fiy += fy; fiz += fz;
+          const int fj = A.fold ? __ldg(A.fold + j) : j;
+          atomicAdd(A.f + 3 * (size_t)fj, -fx);
+          atomicAdd(A.f + 3 * (size_t)fj + 1, -fy);
+          atomicAdd(A.f + 3 * (size_t)fj + 2, -fz);
+          // reference component order: xx yy zz yz zx xy
+          va[0] -= dx * fx; va[1] -= dy * fy; va[2] -= dz * fz;
+          va[3] -= dy * fz; va[4] -= dz * fx; va[5] -= dx * fy;
+        }
+      }
     }
 #pragma unroll
     for (int q = 0; q < 6; ++q) vir[q] += va[q];
@@ -622,7 +868,11 @@ __global__ void __launch_bounds__(kBlock) fused_kernel(const __grid_constant__ K
       atomicAdd(A.f + 3 * (size_t)fi + 2, gz);
     }
     __syncthreads();
+    MLIPG_STAMP(4)
   }
+#undef MLIPG_STAMP
+  if (prof && tid == 0)
+    for (int k = 0; k < 5; ++k) atomicAdd(A.phase_clocks + k, ph[k]);
   // per-CTA partial sums: energy + virial (reference order)
   double vals[7] = {ecta, vir[0], vir[1], vir[2], vir[3], vir[4], vir[5]};
 #pragma unroll

@@ -32,11 +32,15 @@ struct KernelArgs {
   const DeviceTerm* terms;
   const DeviceUnit* units;
   const int* unit_off;    // [T + 1]
+  const DeviceIrrUnit* iunits;  // batched-tuple units
+  const int* iunit_off;          // [T + 1]
+  const DeviceTuple* tuples;
   const DeviceUnit* nl_units;
   const int* nl_off;      // [T + 1]
   const DevicePoly* poly;
   const int* poly_off;    // [T + 1]
   const double* w_lin;    // [n_itc][16]
+  const float* w_lin_f;   // [n_itc][16], FP32 copy for the mixed path
   const double* radial;   // [F][2] (beta, mu)
   int T, F, L, Lh, nb_cap, nl_cap;
   double rc;
@@ -46,6 +50,7 @@ struct KernelArgs {
   double* vatom;          // [ncenters][6] centre virial, LAMMPS order xx yy zz xy xz yz (may be null)
   double* partials;       // [gridDim.x][8]: energy, virial(6, reference order), spare
   int* status;            // [1]
+  unsigned long long* phase_clocks;  // optional [8]: SM cycles spent per phase (P1..P6)
 };
 
 size_t fused_smem_bytes(bool fp64, int T, int Lh, int nb_cap, int nl_cap);

@@ -301,7 +301,7 @@ bool fold_terms(Model& M, std::string& err) {
   return true;
 }
 
-void build_schedules(Model& M) {
+bool build_schedules(Model& M, std::string& err) {
   const int T = M.T, F = M.F;
   // nonlinear itc: appear in any polynomial term of order >= 2
   std::vector<char> is_nl(M.n_itc, 0);
@@ -319,8 +319,9 @@ void build_schedules(Model& M) {
   for (int t = 0; t < T; ++t) {
     Schedule& S = M.sched[t];
     std::vector<int> slot(M.n_itc, -1);
+    // nonlinear slots first (independent of how the itc is evaluated)
     for (int i = 0; i < M.n_itc; ++i) {
-      if (!M.itc[i].inter[t]) continue;
+      if (!M.itc[i].inter[t] || !is_nl[i]) continue;
       const int k = M.itc[i].irreps;
       DeviceUnit u{};
       u.itc = i;
@@ -328,12 +329,71 @@ void build_schedules(Model& M) {
       u.nterm = M.irr_cnterms[k];
       u.q = (uint8_t)M.irr_l[k].size();
       for (int p = 0; p < u.q; ++p) u.s[p] = (uint8_t)M.other_type[M.itc[i].type_combs[p] * T + t];
-      u.nl_slot = -1;
-      if (is_nl[i]) {
-        u.nl_slot = (int)S.nl_units.size();
-        slot[i] = u.nl_slot;
-        S.nl_units.push_back(u);
+      u.nl_slot = (int)S.nl_units.size();
+      slot[i] = u.nl_slot;
+      S.nl_units.push_back(u);
+    }
+    // batched-tuple units for orders <= 3 when T <= 3
+    std::vector<char> covered(M.n_itc, 0);
+    if (T <= 3) {
+      std::map<std::pair<int, std::vector<int>>, int> itc_of;
+      for (int i = 0; i < M.n_itc; ++i) itc_of[{M.itc[i].irreps, M.itc[i].type_combs}] = i;
+      for (int k = 0; k < (int)M.irr_l.size(); ++k) {
+        const auto& lc = M.irr_l[k];
+        const int q = (int)lc.size();
+        if (q > 3) continue;
+        int nt = 1;
+        for (int p = 0; p < q; ++p) nt *= T;
+        const int tup0 = (int)S.tuples.size();
+        for (int j = 0; j < nt; ++j) {
+          std::vector<int> sv(q), tc(q);
+          int r = j;
+          for (int p = q - 1; p >= 0; --p) { sv[p] = r % T; r /= T; }
+          bool canon = true;
+          for (int p = 1; p < q; ++p)
+            if (lc[p] == lc[p - 1] && sv[p] < sv[p - 1]) canon = false;
+          DeviceTuple d{-1, -1};
+          if (canon) {
+            for (int p = 0; p < q; ++p) tc[p] = M.type_pairs[t * T + sv[p]];
+            auto it = itc_of.find({k, tc});
+            if (it != itc_of.end() && M.itc[it->second].inter[t]) {
+              d.itc = it->second;
+              d.nl_slot = slot[it->second];
+              covered[it->second] = 1;
+            }
+          }
+          S.tuples.push_back(d);
+        }
+        // order 3 with 3 elements: one unit per element of slot 0 (T*T tuples each)
+        const bool fix0 = (q == 3 && T == 3);
+        const int nsub = fix0 ? T : 1;
+        for (int s0 = 0; s0 < nsub; ++s0)
+          for (int c0 = 0; c0 < M.irr_cnterms[k]; c0 += kIrrChunk) {
+            DeviceIrrUnit iu{};
+            iu.term0 = M.irr_cfirst[k] + c0;
+            iu.nterm = std::min(kIrrChunk, M.irr_cnterms[k] - c0);
+            iu.tup = tup0 + (fix0 ? s0 * T * T : 0);
+            iu.q = (uint8_t)q;
+            iu.s0 = (uint8_t)s0;
+            S.iunits.push_back(iu);
+          }
       }
+      std::stable_sort(S.iunits.begin(), S.iunits.end(),
+                       [](const DeviceIrrUnit& a, const DeviceIrrUnit& b) {
+                         if (a.nterm * a.q != b.nterm * b.q) return a.nterm * a.q > b.nterm * b.q;
+                         return a.q > b.q;
+                       });
+    }
+    for (int i = 0; i < M.n_itc; ++i) {
+      if (!M.itc[i].inter[t] || covered[i]) continue;
+      const int k = M.itc[i].irreps;
+      DeviceUnit u{};
+      u.itc = i;
+      u.term0 = M.irr_cfirst[k];
+      u.nterm = M.irr_cnterms[k];
+      u.q = (uint8_t)M.irr_l[k].size();
+      for (int p = 0; p < u.q; ++p) u.s[p] = (uint8_t)M.other_type[M.itc[i].type_combs[p] * T + t];
+      u.nl_slot = slot[i];
       S.units.push_back(u);
     }
     // longest units first, grouped by order
@@ -356,7 +416,18 @@ void build_schedules(Model& M) {
       S.poly.push_back(dp);
     }
     (void)F;
+    // every feature valid for this element is evaluated exactly once
+    std::vector<int> seen(M.n_itc, 0);
+    for (const DeviceTuple& d : S.tuples)
+      if (d.itc >= 0) seen[d.itc]++;
+    for (const DeviceUnit& u : S.units) seen[u.itc]++;
+    for (int i = 0; i < M.n_itc; ++i)
+      if (seen[i] != (M.itc[i].inter[t] ? 1 : 0)) {
+        err = "internal error: work schedule does not cover every feature once";
+        return false;
+      }
   }
+  return true;
 }
 
 }  // namespace
@@ -516,8 +587,7 @@ bool build_model(Model& M, std::string& err) {
     M.other_type[tc * M.T + tpm[tc].second] = tpm[tc].first;
   }
   if (!fold_terms(M, err)) return false;
-  build_schedules(M);
-  return true;
+  return build_schedules(M, err);
 }
 
 bool count_coefficients(int n_types, int model_type, int maxp, int maxl, int gtinv_order,

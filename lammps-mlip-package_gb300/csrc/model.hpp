@@ -67,6 +67,25 @@ struct DevicePoly {       // 32 bytes
   int pad;
 };
 
+// All element tuples of one irreps (orders 1..3, up to 3 elements) over a
+// chunk of its canonical terms: the kernel evaluates every tuple of the
+// chunk per term from one set of order-parameter loads.  Tuples are ordered
+// lexicographically over T^q; the DeviceTuple array at `tup` maps each to its
+// itc (or -1 for orderings that are not the canonical multiset order).
+struct DeviceIrrUnit {    // 16 bytes
+  int term0;
+  int nterm;
+  int tup;                // first DeviceTuple of this unit (T^(q-1) of them when s0 is fixed)
+  uint8_t q;
+  uint8_t s0;             // element of slot 0 for order-3 units with 3 elements
+  uint8_t pad[2];
+};
+struct DeviceTuple {      // 8 bytes
+  int itc;                // -1: not a feature (non-canonical ordering)
+  int nl_slot;            // slot among nonlinear features, -1 if linear only
+};
+constexpr int kIrrChunk = 24;  // canonical terms per batched unit
+
 struct ITC {
   int irreps;
   std::vector<int> type_combs;
@@ -74,7 +93,9 @@ struct ITC {
 };
 
 struct Schedule {         // per centre element
-  std::vector<DeviceUnit> units;     // all valid itc, sorted by cost
+  std::vector<DeviceIrrUnit> iunits; // batched-tuple units (T <= 3, order <= 3)
+  std::vector<DeviceTuple> tuples;   // tuple -> itc tables of the batched units
+  std::vector<DeviceUnit> units;     // remaining valid itc, sorted by cost
   std::vector<DeviceUnit> nl_units;  // nonlinear itc, nl_slot = position
   std::vector<DevicePoly> poly;      // order >= 2 polynomial terms
 };

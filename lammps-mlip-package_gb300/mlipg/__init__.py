@@ -70,6 +70,17 @@ def lib():
         "mlipg_nlist_destroy": (None, [P]),
         "mlipg_set_profiling": (i32, [P, i32]),
         "mlipg_kernel_times": (i32, [P, ctypes.POINTER(ctypes.c_float), i32]),
+        "mlipg_phase_cycles": (i32, [P, ctypes.POINTER(ctypes.c_ulonglong)]),
+        "mlipg_md_create": (i32, [P, dp, i32, dp, dp, ip, ctypes.c_double, ctypes.POINTER(P)]),
+        "mlipg_md_run": (i32, [P, i32, ctypes.c_double, i32]),
+        "mlipg_md_state": (i32, [P, dp, dp, dp]),
+        "mlipg_md_thermo": (i32, [P, dp]),
+        "mlipg_md_destroy": (None, [P]),
+        "mlipg_batch_create": (i32, [P, i32, ip, dp, dp, ip, ctypes.POINTER(P)]),
+        "mlipg_batch_launch": (i32, [P]),
+        "mlipg_batch_compute": (i32, [P, dp, dp, dp]),
+        "mlipg_batch_sizes": (i32, [P, ip, llp]),
+        "mlipg_batch_destroy": (None, [P]),
         "mlipg_measure_fma_peak": (i32, [i32, dp]),
     }
     for name, (res, args) in sig.items():
@@ -257,7 +268,118 @@ class Potential:
                                                   nbr_idx, img, cell, center_cell, fold, nb_cap,
                                                   f, eatom, vatom, out8), self.h)
 
+    PHASES = ["compaction", "order_parameters", "nonlinear_polynomial", "invariants_adjoint",
+              "forces_reduction"]
+
+    def phase_cycles(self):
+        buf = (ctypes.c_ulonglong * 8)()
+        _check(lib().mlipg_phase_cycles(self.h, buf), self.h)
+        return dict(zip(self.PHASES, [int(buf[k]) for k in range(5)]))
+
     def device_status(self) -> int:
         b = ctypes.c_int()
         _check(lib().mlipg_device_status(self.h, ctypes.byref(b)), self.h)
         return b.value
+
+
+class MD:
+    """NVE molecular dynamics of one periodic cell on the device (metal units)."""
+
+    THERMO = ["pe", "ke", "temp", "etotal", "press", "pxx", "pyy", "pzz", "pxy", "pxz", "pyz",
+              "rebuilds"]
+
+    def __init__(self, potential: Potential, cell, velocities=None, skin: float = 1.0):
+        self.pot = potential
+        self.n = cell.natoms
+        lat = np.ascontiguousarray(cell.lattice, dtype=np.float64)
+        x = np.ascontiguousarray(cell.positions, dtype=np.float64)
+        t = np.ascontiguousarray(cell.types, dtype=np.int32)
+        v = None if velocities is None else np.ascontiguousarray(velocities, dtype=np.float64)
+        h = ctypes.c_void_p()
+        rc = lib().mlipg_md_create(potential.h, _dp(lat), self.n, _dp(x),
+                                   _dp(v) if v is not None else None, _ip(t), skin,
+                                   ctypes.byref(h))
+        if rc != 0:
+            raise MlipgError(rc, lib().mlipg_last_error(potential.h).decode())
+        self.h = h
+
+    def run(self, nsteps: int, dt: float = 0.001, graph: bool = True):
+        rc = lib().mlipg_md_run(self.h, nsteps, dt, 1 if graph else 0)
+        if rc != 0:
+            raise MlipgError(rc, lib().mlipg_last_error(self.pot.h).decode())
+
+    def state(self):
+        x = np.zeros((self.n, 3))
+        v = np.zeros((self.n, 3))
+        f = np.zeros((self.n, 3))
+        _check(lib().mlipg_md_state(self.h, _dp(x), _dp(v), _dp(f)))
+        return x, v, f
+
+    def thermo(self):
+        o = np.zeros(12)
+        _check(lib().mlipg_md_thermo(self.h, _dp(o)))
+        return dict(zip(self.THERMO, o.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mlipg_md_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def maxwell_boltzmann(masses, temperature, rng):
+    """Velocities (A/ps, metal units) at `temperature` K, zero total momentum,
+    rescaled to exactly that temperature with dof = 3N - 3."""
+    kb, mvv2e = 8.617343e-5, 1.0364269e-4
+    m = np.asarray(masses, dtype=np.float64)
+    v = rng.normal(size=(len(m), 3)) * np.sqrt(kb * temperature / (m * mvv2e))[:, None]
+    v -= (m[:, None] * v).sum(0) / m.sum()
+    ke = 0.5 * (m[:, None] * v * v).sum() * mvv2e
+    t = 2 * ke / ((3 * len(m) - 3) * kb)
+    return v * np.sqrt(temperature / t) if t > 0 else v
+
+
+class Batch:
+    """Many periodic cells evaluated in one persistent launch (see mlipg_batch_*)."""
+
+    def __init__(self, potential: Potential, cells):
+        self.pot = potential
+        self.ncells = len(cells)
+        n = np.array([c.natoms for c in cells], dtype=np.int32)
+        lat = np.ascontiguousarray(np.stack([c.lattice for c in cells]), dtype=np.float64)
+        x = np.ascontiguousarray(np.concatenate([c.positions for c in cells]), dtype=np.float64)
+        t = np.ascontiguousarray(np.concatenate([c.types for c in cells]), dtype=np.int32)
+        self.natoms = n
+        self.offsets = np.concatenate([[0], np.cumsum(n)])
+        h = ctypes.c_void_p()
+        rc = lib().mlipg_batch_create(potential.h, self.ncells, _ip(n), _dp(lat), _dp(x), _ip(t),
+                                      ctypes.byref(h))
+        if rc != 0:
+            raise MlipgError(rc, "mlipg_batch_create failed")
+        self.h = h
+        na = ctypes.c_int()
+        npairs = ctypes.c_longlong()
+        lib().mlipg_batch_sizes(self.h, ctypes.byref(na), ctypes.byref(npairs))
+        self.total_atoms, self.npairs = na.value, npairs.value
+
+    def launch(self):
+        _check(lib().mlipg_batch_launch(self.h))
+
+    def compute(self):
+        e = np.zeros(self.ncells)
+        f = np.zeros((self.total_atoms, 3))
+        v = np.zeros((self.ncells, 6))
+        rc = lib().mlipg_batch_compute(self.h, _dp(e), _dp(f), _dp(v))
+        if rc != 0:
+            raise MlipgError(rc, lib().mlipg_last_error(self.pot.h).decode())
+        return e, f, v
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mlipg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

@@ -50,6 +50,8 @@ def _sources():
         "kernels_common.o": ("nvcc", os.path.join(CSRC, "kernels_common.cu")),
         "peak.o": ("nvcc", os.path.join(CSRC, "peak.cu")),
         "noalloc.o": ("nvcc", os.path.join(CSRC, "noalloc.cu")),
+        "md.o": ("nvcc", os.path.join(CSRC, "md.cu")),
+        "batch.o": ("nvcc", os.path.join(CSRC, "batch.cu")),
         "kernels_f64.o": ("nvcc", os.path.join(CSRC, "kernels_f64.cu")),
         "kernels_f32.o": ("nvcc", os.path.join(CSRC, "kernels_f32.cu")),
     }
@@ -79,8 +81,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
             cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-Wall", "-c", src, "-o",
                    out] + inc
         else:
-            cmd = [nvcc] + ARCH + ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
-                                   "-c", src, "-o", out] + inc
+            cmd = [nvcc] + ARCH + ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler",
+                                   "-fPIC,-fopenmp", "-c", src, "-o", out] + inc
             if verbose:
                 cmd += ["-Xptxas", "-v"]
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE,

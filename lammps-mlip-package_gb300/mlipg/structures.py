@@ -184,11 +184,12 @@ def random_types(cell: Cell, ntypes: int, rng: np.random.Generator) -> Cell:
 
 def random_triclinic_cell(natoms: int, density: float, ntypes: int,
                           rng: np.random.Generator, min_dist: float = 1.8,
-                          max_tries: int = 200000) -> Cell:
+                          max_rounds: int = 2000) -> Cell:
     """Random cell matrix with angles U(60, 120) deg at the given number density.
 
-    Atoms are placed uniformly with minimum-image distance rejection.  Cells
-    whose matrix is nearly degenerate are redrawn.
+    Atoms are uniform in the cell, then every atom closer than `min_dist`
+    (minimum image) to an earlier atom is redrawn until no pair violates the
+    distance.  Cells whose matrix is nearly degenerate are redrawn.
     """
     vol = natoms / density
     while True:
@@ -206,26 +207,28 @@ def random_triclinic_cell(natoms: int, density: float, ntypes: int,
         if np.min(_perp_widths(lat)) < 0.35 * s:
             continue
         break
-    inv = np.linalg.inv(lat)
-    pos = np.zeros((natoms, 3))
-    k = 0
-    tries = 0
-    while k < natoms:
-        tries += 1
-        if tries > max_tries:
-            raise RuntimeError("could not place atoms with the minimum distance")
-        f = rng.random(3)
-        p = f @ lat
-        if k > 0:
-            d = (pos[:k] - p) @ inv
-            d -= np.round(d)
-            dc = d @ lat
-            if np.min(np.einsum("ij,ij->i", dc, dc)) < min_dist * min_dist:
-                continue
-        pos[k] = p
-        k += 1
+    frac = rng.random((natoms, 3))
+    md2 = min_dist * min_dist
+
+    def min_r2(ids):
+        d = frac[ids][:, None, :] - frac[None, :, :]
+        d -= np.round(d)
+        dc = d @ lat
+        r2 = np.einsum("ijk,ijk->ij", dc, dc)
+        r2[np.arange(len(ids)), ids] = np.inf
+        return r2
+
+    r2 = min_r2(np.arange(natoms))
+    bad = np.nonzero(np.triu(r2 < md2, k=1).any(axis=0))[0]   # clashes with an earlier atom
+    for _ in range(max_rounds):
+        if bad.size == 0:
+            break
+        frac[bad] = rng.random((bad.size, 3))
+        bad = bad[(min_r2(bad) < md2).any(axis=1)]
+    else:
+        raise RuntimeError("could not place atoms with the minimum distance")
     types = np.asarray(rng.integers(0, ntypes, natoms), dtype=np.int32)
-    return Cell(lat, pos, types)
+    return Cell(lat, frac @ lat, types)
 
 
 def read_lammps_data(path: str) -> Cell:

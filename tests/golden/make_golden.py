@@ -42,12 +42,31 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 POTS = ["gtinv-197", "gtinv-820", "gtinv-434"]
 STRUCTS = ["structure.lammps", "structure_00064_conventional.lammps",
            "structure_00064_triclinic.lammps"]
+DUMPS = ["dump.atom.gtinv-197", "dump.atom.gtinv-820", "dump.atom.gtinv-434"]
 SH_DIRS = [(0.3, -0.4, 1.2), (-1.1, 0.2, -0.5), (0.7, 0.7, 0.0), (0.0, 0.0, 2.0),
            (1e-3, -2e-3, -1.5), (-0.25, -0.9, 0.35)]
 
 
 def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a, dtype=np.int64).tobytes()).hexdigest()
+
+
+def thermo_rows(log_path):
+    """All thermo rows of the first run block: {step: {column: value}}."""
+    lines = open(log_path).read().splitlines()
+    for i, ln in enumerate(lines):
+        if ln.strip().startswith("Step "):
+            head = ln.split()
+            rows = {}
+            for k in range(i + 1, len(lines)):
+                if lines[k].startswith("Loop time"):
+                    break
+                vals = lines[k].split()
+                rows[int(float(vals[0]))] = dict(zip(head, map(float, vals)))
+                rows[int(float(vals[0]))]["cite"] = "test/regression/%s:%d" % (
+                    os.path.basename(log_path), k + 1)
+            return rows
+    raise ValueError("no thermo block in " + log_path)
 
 
 def thermo_step0(log_path):
@@ -118,7 +137,7 @@ def main():
         with open(os.path.join(reg, p + ".mlip"), "rb") as fi, \
                 gzip.open(os.path.join(HERE, p + ".mlip.gz"), "wb", 9) as fo:
             shutil.copyfileobj(fi, fo)
-    for s in STRUCTS:
+    for s in STRUCTS + DUMPS:
         shutil.copy(os.path.join(reg, s), os.path.join(HERE, s))
 
     gold = {"source": "quantum-mtl/lammps-mlip-package test/regression and test/*.cpp"}
@@ -132,6 +151,16 @@ def main():
         vals["cite"] = "test/regression/%s:%d" % (log, line)
         logs[name] = vals
     gold["thermo_step0"] = logs
+    # NVE trajectories: thermo at every printed step (100 steps, dt 1 fs; the
+    # stress run uses dt 5 fs and prints every 50 steps)
+    traj = {}
+    for name, log, dt in [("gtinv-197", "log.lammps.gtinv-197", 0.001),
+                          ("gtinv-820", "log.lammps.gtinv-820", 0.001),
+                          ("gtinv-434", "log.lammps.gtinv-434", 0.001),
+                          ("gtinv-197-stress", "log.lammps.gtinv-197.stress.ev_tally", 0.005)]:
+        rows = thermo_rows(os.path.join(reg, log))
+        traj[name] = {"dt": dt, "rows": {str(k): v for k, v in rows.items()}}
+    gold["nve"] = traj
 
     L = ref_lib(ref)
     gold["model"] = {p: model_fingerprint(L, os.path.join(reg, p + ".mlip")) for p in POTS}

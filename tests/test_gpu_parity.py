@@ -4,10 +4,10 @@ Tolerances:
 * FP64 path: energy, every force component and the virial agree with the
   oracle to 1e-10 relative (to the largest magnitude of each quantity);
   only the summation order differs.
-* mixed path: energy error <= 1e-6 eV/atom on the synthetic workload
-  potentials and force RMS error <= 1e-4 eV/A against the FP64 oracle; on the
-  regression potentials (coefficients up to 1e5) the stated bound is a
-  relative one, 2e-5 of the force scale.
+* mixed path: force RMS error <= 1e-4 eV/A against the FP64 oracle on every
+  potential; energy error <= 1e-6 eV/atom on the synthetic workload
+  potentials and <= 2e-5 of the per-atom energy scale on the regression
+  potentials (coefficients up to 1e5).
 """
 import numpy as np
 import pytest
@@ -77,8 +77,9 @@ def test_regression_potentials_mixed(potdir, pot):
     ref = o.compute(s)
     got = mlipg.Potential(potdir[pot], mlipg.PREC_MIXED).compute(s)
     F, Fr = s.fold_forces(got["f_all"]), s.fold_forces(ref["f_all"])
-    scale = np.abs(Fr).max()
-    assert np.sqrt(np.mean((F - Fr) ** 2)) <= 2e-5 * scale
+    # the stated accuracy of the mixed path: force RMS <= 1e-4 eV/A; energies of these
+    # potentials (coefficients up to 1e5) within 2e-5 of the per-atom energy scale
+    assert np.sqrt(np.mean((F - Fr) ** 2)) <= 1e-4
     assert abs(got["energy"] - ref["energy"]) / s.nlocal <= 2e-5 * np.abs(ref["eatom"]).max()
 
 
