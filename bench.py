@@ -52,6 +52,15 @@ WORKLOADS = {
     "bcc-binary-16k": dict(lattice="bcc", n=20, a=3.2, ntypes=2, jitter=0.05,
                            pot="bcc-binary-16k"),
     "fcc-al-256": dict(lattice="fcc", n=4, a=4.05, ntypes=1, jitter=0.05, pot="fcc-al-256"),
+    # 4096 random triclinic cells, 8..512 atoms (log-uniform), one persistent launch
+    "triclinic-batch-4096": dict(kind="batch", cells=4096, lo=8, hi=512, density=0.06,
+                                 ntypes=2, pot="triclinic-batch"),
+    # Poisson stream of requests (16..8192 atoms, FP64/mixed 50/50) at 80% of capacity
+    "serve-poisson": dict(kind="serve", requests=20000, lo=16, hi=8192, density=0.06,
+                          ntypes=2, pot="triclinic-batch", load=0.8, budget=64 << 30),
+    # 50 NVE steps of the 1M-atom ternary alloy at 300 K, each step a CUDA graph
+    "md-fcc-ternary-1m": dict(kind="md", lattice="fcc", n=64, a=4.0, ntypes=3, jitter=0.1,
+                              pot="fcc-ternary-1m", temperature=300.0, dt=0.001),
 }
 POT_DESC = {
     "fcc-ternary-1m": "3 elements, rc 6, 15 Gaussians, gtinv order 4 l<=[12,8,4], "
@@ -60,6 +69,8 @@ POT_DESC = {
                       "model_type 3 max_p 2, 14340 coefficients ~N(0,1e-3)",
     "fcc-al-256": "1 element, rc 6, 10 Gaussians, gtinv order 3 l<=[4,4], model_type 2 "
                   "max_p 2, 20300 coefficients ~N(0,1e-3)",
+    "triclinic-batch": "2 elements, rc 6, 15 Gaussians, gtinv order 3 l<=[12,8], "
+                       "model_type 3 max_p 2, 11805 coefficients ~N(0,1e-3)",
 }
 SKIN = 1.0
 
@@ -167,6 +178,8 @@ def run_reference(args, dist):
     if dist["rank"] != 0:
         return
     spec = WORKLOADS[args.workload]
+    if spec.get("kind") in ("batch", "serve"):
+        return run_reference_cells(args, dist, spec)
     with tempfile.TemporaryDirectory() as d:
         pot = os.path.join(d, "pot.mlip")
         workload_potential(pot, spec["pot"])
@@ -194,12 +207,39 @@ def run_reference(args, dist):
                 "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": args.workload, "atoms": sysm.nlocal,
-                           "potential": POT_DESC[args.workload],
+                           "potential": POT_DESC[spec["pot"]],
                            "sample_per_step": per_step},
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
                                  "sample": "%d random centres per step of the %d-atom workload"
                                            % (per_step, sysm.nlocal)},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+
+
+def run_reference_cells(args, dist, spec):
+    """--impl reference for the many-cell workloads: the CPU implementation on
+    whole cells drawn from the workload, each step a bounded time slice."""
+    from mlipg.potential import workload_potential
+    with tempfile.TemporaryDirectory() as d:
+        pot = os.path.join(d, "pot.mlip")
+        workload_potential(pot, spec["pot"])
+        n = 256 if spec["kind"] == "batch" else 64
+        cells = triclinic_cells(n, spec["lo"], spec["hi"], spec["density"], spec["ntypes"],
+                                seed=7 if spec["kind"] == "batch" else 17)
+        per_step = max(1.0, min(8.0, 90.0 / max(args.steps + args.warmup, 1)))
+        for w in range(args.warmup):
+            cpu_baseline_cells(pot, cells, 0.5, seed=100 + w)
+        vals = [cpu_baseline_cells(pot, cells, per_step, seed=w) for w in range(args.steps)]
+        atoms_per_s = float(np.mean([v["value"] for v in vals]))
+        line = {"impl": "reference", "metric": METRIC, "value": atoms_per_s, "unit": UNIT,
+                "n_gpus": dist["world"], "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": per_step * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": args.workload, "potential": POT_DESC[spec["pot"]],
+                           "sample_per_step": "%.1f s of whole cells" % per_step},
+                "cpu_baseline": dict(vals[0], value=atoms_per_s),
+                "e2e": {"value": atoms_per_s, "unit": UNIT, "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
 
@@ -390,7 +430,7 @@ def run_ours(args, dist):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic",
                 "config": {"workload": args.workload, "atoms_per_gpu": natoms,
-                           "potential": POT_DESC[args.workload],
+                           "potential": POT_DESC[spec["pot"]],
                            "precision": "mixed: FP32 radial/Y_lm/invariant/adjoint products, "
                                         "FP64 a_nlm sums, forces, energies, virial",
                            "neighbours_in_cutoff_per_atom":
@@ -412,6 +452,314 @@ def run_ours(args, dist):
     g.close()
 
 
+# ---------------------------------------------------------------- other configurations
+
+def triclinic_cells(count, lo, hi, density, ntypes, seed):
+    """`count` random triclinic cells, atom counts log-uniform in [lo, hi]."""
+    from mlipg.structures import random_triclinic_cell
+    rng = np.random.default_rng(seed)
+    sizes = np.minimum(hi, np.exp(rng.uniform(np.log(lo), np.log(hi + 1), count)).astype(int))
+    return [random_triclinic_cell(int(k), density, ntypes, rng) for k in sizes]
+
+
+def cpu_baseline_cells(pot_path, cells, seconds, seed=0):
+    """CPU oracle (all host threads) on whole cells drawn at random from `cells`."""
+    import mlipg
+    from oracle import Oracle
+    nth = host_threads()
+    o = Oracle(pot_path, threads=nth)
+    rng = np.random.default_rng(seed)
+    atoms, t, ncell = 0, 0.0, 0
+    for k in rng.permutation(len(cells)):
+        sysm = mlipg.native_system(cells[k], 6.0, 0.0)
+        t0 = time.perf_counter()
+        o.compute(sysm)
+        t += time.perf_counter() - t0
+        atoms += sysm.nlocal
+        ncell += 1
+        if t >= seconds:
+            break
+    return {"value": atoms / t, "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": "%d whole cells (%d atoms) of the workload, one evaluation each "
+                      "(%.1f s)" % (ncell, atoms, t)}
+
+
+def type_flops(g, cells_types, nb_mean):
+    t = np.concatenate(cells_types)
+    return sum(int(np.sum(t == k)) * g.flops_per_atom_step(int(k), nb_mean) for k in np.unique(t))
+
+
+def run_batch(args, dist):
+    """Every cell of the batch evaluated (energy, forces, stress) in one launch."""
+    import torch
+
+    import mlipg
+    from mlipg.potential import workload_potential
+    spec = WORKLOADS[args.workload]
+    rank = dist["rank"]
+    tmp = tempfile.mkdtemp()
+    pot = os.path.join(tmp, "pot.mlip")
+    workload_potential(pot, spec["pot"])
+    cells = triclinic_cells(spec["cells"], spec["lo"], spec["hi"], spec["density"],
+                            spec["ntypes"], seed=7 + rank)
+    natoms = sum(c.natoms for c in cells)
+    cpu = cpu_baseline_cells(pot, cells, args.cpu_seconds) \
+        if rank == 0 and args.cpu_seconds > 0 else None
+    dev = torch.device("cuda", 0)
+    res, rates, kms, create_s = {}, {}, {}, {}
+    clk = None
+    for prec in (mlipg.PREC_FP64, mlipg.PREC_MIXED):
+        g = mlipg.Potential(pot, prec)
+        stream = torch.cuda.ExternalStream(g.stream(), device=dev)
+        t0 = time.perf_counter()
+        b = mlipg.Batch(g, cells)
+        create_s[prec] = time.perf_counter() - t0
+        for _ in range(args.warmup):
+            b.launch()
+        torch.cuda.synchronize()
+        g.kernel_times()
+        g.set_profiling(True)
+        clocks = ClockSampler(0)
+        clocks.start()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            b.launch()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        c = clocks.stop()
+        g.set_profiling(False)
+        el = ev0.elapsed_time(ev1)
+        if dist["world"] > 1:
+            t = torch.tensor([el], dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        rates[prec] = natoms * args.steps * dist["world"] / (el * 1e-3)
+        kt = [t for t in g.kernel_times() if t > 0]
+        kms[prec] = float(np.mean(kt)) if kt else float("nan")
+        res[prec] = b.compute()
+        npairs = b.npairs
+        if prec == mlipg.PREC_MIXED:
+            clk = c
+            el_mixed = el
+            # e2e: the public batch API from host cells each step (neighbour
+            # lists, upload, launch, results back)
+            t0 = time.perf_counter()
+            ne2e = max(1, min(args.steps, 3))
+            for _ in range(ne2e):
+                bb = mlipg.Batch(g, cells)
+                bb.compute()
+                bb.close()
+            e2e_s = (time.perf_counter() - t0) / ne2e
+            nb_mean = npairs / natoms
+            flops = type_flops(g, [c.types for c in cells], nb_mean)
+            peak = mlipg.measure_fma_peak(False)
+            ach = flops / (kms[prec] * 1e-3) / 1e12
+            roof = {"bound": "fp32-cuda-core", "achieved": ach, "peak": peak,
+                    "unit": "TFLOP/s", "frac": ach / peak, "traffic": None,
+                    "peak_source": "live FP32 FMA microkernel on this GPU",
+                    "kernel": "fused kernel (mixed), all cells", "kernel_ms": kms[prec],
+                    "algorithmic_flops_per_launch": flops}
+        b.close()
+        g.close()
+    e64, f64, v64 = res[mlipg.PREC_FP64]
+    e32, f32, v32 = res[mlipg.PREC_MIXED]
+    n = np.array([c.natoms for c in cells])
+    acc = {"force_rms_err_eV_per_A": float(np.sqrt(np.mean((f32 - f64) ** 2))),
+           "force_rms_eV_per_A": float(np.sqrt(np.mean(f64 ** 2))),
+           "energy_err_eV_per_atom_max": float(np.max(np.abs(e32 - e64) / n)),
+           "virial_err_max_eV": float(np.abs(v32 - v64).max())}
+    if rank == 0:
+        h2d = natoms * (32 + 4 + 4 + 4 + 4) + 8 * npairs + len(cells) * (72 + 4)
+        line = {"metric": METRIC, "value": rates[mlipg.PREC_MIXED], "unit": UNIT,
+                "n_gpus": dist["world"], "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": el_mixed / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": args.workload, "cells": len(cells), "atoms": natoms,
+                           "atoms_per_cell": "log-uniform [%d, %d], mean %.1f"
+                                             % (spec["lo"], spec["hi"], natoms / len(cells)),
+                           "cells_desc": "random triclinic, angles U(60,120) deg, density "
+                                         "0.06/A^3, 1.8 A minimum distance, 2 species",
+                           "potential": POT_DESC[spec["pot"]],
+                           "neighbours_per_atom": npairs / natoms,
+                           "l2": "inputs larger than L2 (%.0f MB)" % (h2d / 1e6),
+                           "step": "one persistent launch over all cells + per-cell sums"},
+                "fp64": {"value": rates[mlipg.PREC_FP64], "unit": UNIT,
+                         "kernel_ms": kms[mlipg.PREC_FP64],
+                         "mixed_over_fp64": rates[mlipg.PREC_MIXED] / rates[mlipg.PREC_FP64]},
+                "accuracy_mixed_vs_fp64": acc,
+                "e2e": {"value": natoms * dist["world"] / e2e_s, "unit": UNIT,
+                        "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(24 * natoms + 56 * len(cells)),
+                        "api": "mlipg_batch_create + mlipg_batch_compute from host cells "
+                               "(neighbour lists built on the host each step)",
+                        "host_setup_s": create_s[mlipg.PREC_MIXED]},
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+                "gpu_launches": 3 * args.steps}
+        print(json.dumps(line), flush=True)
+
+
+def run_serve(args, dist):
+    """Poisson request stream against the continuous-batching server."""
+    import mlipg
+    from mlipg.potential import workload_potential
+    spec = WORKLOADS[args.workload]
+    rank = dist["rank"]
+    tmp = tempfile.mkdtemp()
+    pot = os.path.join(tmp, "pot.mlip")
+    workload_potential(pot, spec["pot"])
+    nreq = args.requests or spec["requests"]
+    pool = triclinic_cells(args.pool, spec["lo"], spec["hi"], spec["density"], spec["ntypes"],
+                           seed=17 + rank)
+    rng = np.random.default_rng(5 + rank)
+    pick = rng.integers(0, len(pool), nreq)
+    prec = np.where(rng.random(nreq) < 0.5, mlipg.PREC_FP64, mlipg.PREC_MIXED)
+    cpu = cpu_baseline_cells(pot, pool, args.cpu_seconds) \
+        if rank == 0 and args.cpu_seconds > 0 else None
+
+    def burst(srv, idx):
+        t0 = time.perf_counter()
+        tk = [srv.submit(pool[pick[k]], int(prec[k])) for k in idx]
+        for t in tk:
+            srv.wait(t, 600000)
+        return time.perf_counter() - t0
+
+    # capacity: a closed burst of requests drawn like the stream
+    srv = mlipg.Server(pot, budget_bytes=spec["budget"], max_batch_atoms=args.max_batch_atoms)
+    burst(srv, range(min(nreq, 4 * args.warmup)))
+    ncap = min(nreq, max(200, nreq // 20))
+    tcap = burst(srv, range(ncap))
+    cap_atoms = sum(pool[pick[k]].natoms for k in range(ncap)) / tcap
+    cap_req = ncap / tcap
+    srv.close()
+
+    # the stream: exponential inter-arrival gaps at `load` x capacity
+    lam = spec["load"] * cap_req
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, nreq))
+    srv = mlipg.Server(pot, budget_bytes=spec["budget"], max_batch_atoms=args.max_batch_atoms)
+    tickets = [None] * nreq
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+
+    def submitter():
+        for k in range(nreq):
+            d = t0 + arrivals[k] - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            tickets[k] = srv.submit(pool[pick[k]], int(prec[k]))
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    for k in range(nreq):
+        while tickets[k] is None:
+            time.sleep(0.0005)
+        srv.wait(tickets[k], 600000)
+    el = time.perf_counter() - t0
+    th.join()
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    atoms = int(sum(pool[pick[k]].natoms for k in range(nreq)))
+    if rank == 0:
+        nb = spec["density"] * 4.0 / 3.0 * np.pi * 6.0 ** 3
+        h2d = atoms / nreq * (48 + 8 * nb)
+        line = {"metric": METRIC, "value": st["atom_steps_per_s"] * dist["world"], "unit": UNIT,
+                "n_gpus": dist["world"], "steps": nreq, "warmup": args.warmup,
+                "ms_per_step": el / nreq * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+                "config": {"workload": args.workload, "requests": nreq,
+                           "atoms_per_request": "log-uniform [%d, %d], mean %.0f"
+                                                % (spec["lo"], spec["hi"], atoms / nreq),
+                           "structures": "pool of %d random triclinic cells (density 0.06/A^3,"
+                                         " 1.8 A minimum distance, 2 species), drawn at "
+                                         "random per request" % len(pool),
+                           "precision_mix": "FP64 / mixed 50/50 per request",
+                           "potential": POT_DESC[spec["pot"]],
+                           "budget_bytes": spec["budget"],
+                           "max_batch_atoms": args.max_batch_atoms,
+                           "offered_load": spec["load"],
+                           "step": "one request (energy + forces + stress)"},
+                "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"]},
+                "capacity": {"atom_steps_per_s": cap_atoms, "requests_per_s": cap_req,
+                             "burst_requests": ncap},
+                "offered_requests_per_s": lam, "batches": st["batches"],
+                "e2e": {"value": atoms / el, "unit": UNIT,
+                        "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(24 * atoms / nreq + 56),
+                        "api": "mlipg_server_submit / mlipg_server_wait with host arrays"},
+                "roofline": None, "cpu_baseline": cpu, "clocks": clk,
+                "gpu_launches": int(3 * st["batches"])}
+        print(json.dumps(line), flush=True)
+
+
+def run_md(args, dist):
+    """NVE molecular dynamics (velocity Verlet), each step one CUDA graph."""
+    import torch
+
+    import mlipg
+    from mlipg.potential import workload_potential
+    spec = WORKLOADS[args.workload]
+    rank = dist["rank"]
+    tmp = tempfile.mkdtemp()
+    pot = os.path.join(tmp, "pot.mlip")
+    workload_potential(pot, spec["pot"])
+    cell = make_cell(spec, seed=1 + rank)
+    g = mlipg.Potential(pot, mlipg.PREC_MIXED)
+    masses = np.array(g.masses)[cell.types]
+    v = mlipg.maxwell_boltzmann(masses, spec["temperature"], np.random.default_rng(3 + rank))
+    t0 = time.perf_counter()
+    md = mlipg.MD(g, cell, v, skin=SKIN)
+    setup_s = time.perf_counter() - t0
+    md.run(args.warmup, spec["dt"], True)
+    th0 = md.thermo()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    md.run(args.steps, spec["dt"], True)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    clk = clocks.stop()
+    th1 = md.thermo()
+    if dist["world"] > 1:
+        t = torch.tensor([el], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        el = float(t.item())
+    n = cell.natoms
+    value = n * args.steps * dist["world"] / el
+    nb = 4 * 4.0 / 3.0 * np.pi * 6.0 ** 3 / spec["a"] ** 3
+    flops = type_flops(g, [cell.types], nb)
+    peak = mlipg.measure_fma_peak(False)
+    ach = flops / (el / args.steps) / 1e12
+    md.close()
+    g.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist["world"],
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": args.workload, "atoms": n,
+                           "potential": POT_DESC[spec["pot"]],
+                           "md": "NVE velocity Verlet, dt %.3f ps, %g K Maxwell-Boltzmann, "
+                                 "skin %.1f A, list rebuilt when an atom moves skin/2"
+                                 % (spec["dt"], spec["temperature"], SKIN),
+                           "step": "one CUDA graph per step (integrate, forces, integrate, "
+                                   "displacement check)"},
+                "thermo_start": th0, "thermo_end": th1,
+                "energy_drift_eV_per_atom": (th1["etotal"] - th0["etotal"]) / n,
+                "e2e": {"value": n * args.steps * dist["world"] / (el + setup_s), "unit": UNIT,
+                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8,
+                        "api": "mlipg_md_create + mlipg_md_run (setup amortised over the run)"},
+                "roofline": {"bound": "fp32-cuda-core", "achieved": ach, "peak": peak,
+                             "unit": "TFLOP/s", "frac": ach / peak, "traffic": None,
+                             "note": "whole MD step time (upper bound of the force kernel)"},
+                "cpu_baseline": None, "clocks": clk, "gpu_launches": None}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -425,6 +773,11 @@ def main():
                     help="evaluate only the first N centres per step (profiling runs)")
     ap.add_argument("--device-only", action="store_true",
                     help="time the device-resident step only (no e2e/FP64/accuracy/CPU legs)")
+    ap.add_argument("--requests", type=int, default=0,
+                    help="serving: number of requests (default: the workload's)")
+    ap.add_argument("--pool", type=int, default=256,
+                    help="serving: distinct structures the requests are drawn from")
+    ap.add_argument("--max-batch-atoms", type=int, default=65536)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -434,8 +787,15 @@ def main():
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         torch.distributed.init_process_group("gloo")
     try:
+        kind = WORKLOADS[args.workload].get("kind", "cell")
         if args.impl == "reference":
             run_reference(args, dist)
+        elif kind == "batch":
+            run_batch(args, dist)
+        elif kind == "serve":
+            run_serve(args, dist)
+        elif kind == "md":
+            run_md(args, dist)
         else:
             run_ours(args, dist)
     finally:

@@ -180,15 +180,61 @@ int mlipg_measure_fma_peak(int fp64, double* tflops);
  * everything once.  mlipg_batch_compute evaluates all cells: energies[ncells]
  * (eV), forces[natoms_total*3] (eV/A) and virials[ncells*6] (LAMMPS order)
  * back on the host; mlipg_batch_launch only enqueues the evaluation on the
- * handle's stream.  No counterpart in the reference (one structure per
+ * handle's stream and mlipg_batch_results copies the results of the last
+ * launch (waiting for it); mlipg_batch_device_bytes is its device footprint.  No counterpart in the reference (one structure per
  * MLIPModel::set_structure call, mlipkk.cpp:278-372). */
 typedef struct mlipg_batch mlipg_batch;
 int mlipg_batch_create(mlipg_handle* h, int ncells, const int* natoms, const double* lattices,
                        const double* x, const int* elements, mlipg_batch** out);
 int mlipg_batch_launch(mlipg_batch* b);
 int mlipg_batch_compute(mlipg_batch* b, double* energies, double* forces, double* virials);
+int mlipg_batch_results(mlipg_batch* b, double* energies, double* forces, double* virials);
+size_t mlipg_batch_device_bytes(const mlipg_batch* b);
 int mlipg_batch_sizes(const mlipg_batch* b, int* natoms, long long* npairs);
+/* Autotunes the handle's tile shape on this batch (see mlipg_autotune). */
+int mlipg_batch_autotune(mlipg_batch* b, int max_report, double* report, int* nreport);
 void mlipg_batch_destroy(mlipg_batch* b);
+
+/* Tile shape of the fused kernel and its autotuner.  No counterpart in the
+ * reference (its Kokkos team sizes are fixed at compile time).
+ * irr_chunk: coupling terms per batched work unit (even, 2..4096; default 24);
+ * warp_order: 0 = units dealt round robin to the CTA's 8 warps in cost order,
+ *             1 = longest first onto the least-loaded warp;
+ * ctas_per_sm: CTAs per SM of the persistent grid (0 = as many as fit).
+ * Results agree between tilings to rounding (the energy summation is grouped
+ * by unit).  mlipg_set_tiling waits for the handle's stream and re-uploads the
+ * schedules; MD objects re-capture their step graph afterwards.
+ * mlipg_autotune times every candidate (irr_chunk 12/24/48 x both orders x
+ * 1..resident CTAs/SM) on up to 16 centres per resident CTA of the given
+ * structure (same arguments as mlipg_compute_device), keeps the fastest and
+ * writes rows [irr_chunk, warp_order, ctas_per_sm, ms] to report (up to
+ * max_report rows; *nreport = rows timed).  d_f and d_out8 are overwritten. */
+int mlipg_set_tiling(mlipg_handle* h, int irr_chunk, int warp_order, int ctas_per_sm);
+int mlipg_get_tiling(const mlipg_handle* h, int* out3);
+int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4, const int* d_centers,
+                   const int* d_nbr_off, const int* d_nbr_idx, const int* d_img,
+                   const double* d_cell, const int* d_center_cell, int nb_cap, double* d_f,
+                   double* d_out8, int max_report, double* report, int* nreport);
+
+/* Serving: energy + force + stress requests for periodic structures of any
+ * size, evaluated by continuous batching.  Requests (mlipg_server_submit,
+ * thread-safe) are admitted in arrival order against a device-memory budget,
+ * grouped by precision into batches of at most max_batch_atoms atoms and
+ * launched as they arrive; FP64 and mixed batches run on separate streams.
+ * mlipg_server_wait returns a request's energy, forces[natoms*3] and virial
+ * (LAMMPS order) or MLIPG_ETIMEDOUT at its deadline.  A request's energy
+ * does not depend on the other requests in its batch.
+ * mlipg_server_stats: [completed, p50 ms, p99 ms, atom-steps/s, batches,
+ * device bytes in use, queued, in flight].  No counterpart in the reference. */
+typedef struct mlipg_server mlipg_server;
+int mlipg_server_create(const char* potential_path, size_t device_budget_bytes,
+                        int max_batch_atoms, mlipg_server** out);
+int mlipg_server_submit(mlipg_server* s, int natoms, const double* lattice9, const double* x,
+                        const int* elements, int precision, long long* ticket);
+int mlipg_server_wait(mlipg_server* s, long long ticket, int timeout_ms, double* energy,
+                      double* forces, double* virial6);
+int mlipg_server_stats(mlipg_server* s, double* out8);
+void mlipg_server_destroy(mlipg_server* s);
 
 /* NVE molecular dynamics on the device (velocity Verlet as LAMMPS `fix nve`,
  * metal units: A, ps, eV, g/mol; masses from the potential file).  Positions

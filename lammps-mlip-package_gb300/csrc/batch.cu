@@ -40,12 +40,19 @@ __global__ void k_cell_sums(const int* __restrict__ off, const double* __restric
   if (threadIdx.x < 7) out7[7 * (size_t)c + threadIdx.x] = red[threadIdx.x][0];
 }
 
+// Stream-ordered device buffer: allocated and freed on the batch's stream
+// from the device's memory pool, so creating and retiring batches never
+// synchronises the device (other streams keep running).
 template <typename T>
 struct Dev {
   T* p = nullptr;
-  cudaError_t alloc(size_t n) { return cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)); }
+  cudaStream_t s = nullptr;
+  cudaError_t alloc(size_t n, cudaStream_t stream) {
+    s = stream;
+    return cudaMallocAsync(reinterpret_cast<void**>(&p), std::max<size_t>(n, 1) * sizeof(T), s);
+  }
   ~Dev() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, s);
   }
 };
 
@@ -112,6 +119,15 @@ extern "C" int mlipg_batch_create(mlipg_handle* h, int ncells, const int* natoms
     c_x[c] = std::move(xa);
   }
   if (err != MLIPG_OK) return err;
+  {
+    // keep freed batch memory in the pool (a serving loop reuses it at once)
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      unsigned long long keep = ~0ULL;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
   mlipg_batch* b = new mlipg_batch();
   b->h = h;
   b->s = s;
@@ -144,14 +160,15 @@ extern "C" int mlipg_batch_create(mlipg_handle* h, int ncells, const int* natoms
   }
   hoff[N] = (int)b->npairs;
   b->nb_cap = maxn;
-  bool ok = b->x4.alloc(N) == cudaSuccess && b->centers.alloc(N) == cudaSuccess &&
-            b->off.alloc(N + 1) == cudaSuccess && b->idx.alloc(b->npairs) == cudaSuccess &&
-            b->img.alloc(b->npairs) == cudaSuccess && b->ccell.alloc(N) == cudaSuccess &&
-            b->d_cell_off.alloc(ncells + 1) == cudaSuccess &&
-            b->lat.alloc(9 * (size_t)ncells) == cudaSuccess &&
-            b->f.alloc(3 * (size_t)N) == cudaSuccess && b->eatom.alloc(N) == cudaSuccess &&
-            b->vatom.alloc(6 * (size_t)N) == cudaSuccess && b->out8.alloc(8) == cudaSuccess &&
-            b->cell7.alloc(7 * (size_t)ncells) == cudaSuccess;
+  bool ok = b->x4.alloc(N, s) == cudaSuccess && b->centers.alloc(N, s) == cudaSuccess &&
+            b->off.alloc(N + 1, s) == cudaSuccess && b->idx.alloc(b->npairs, s) == cudaSuccess &&
+            b->img.alloc(b->npairs, s) == cudaSuccess && b->ccell.alloc(N, s) == cudaSuccess &&
+            b->d_cell_off.alloc(ncells + 1, s) == cudaSuccess &&
+            b->lat.alloc(9 * (size_t)ncells, s) == cudaSuccess &&
+            b->f.alloc(3 * (size_t)N, s) == cudaSuccess && b->eatom.alloc(N, s) == cudaSuccess &&
+            b->vatom.alloc(6 * (size_t)N, s) == cudaSuccess &&
+            b->out8.alloc(8, s) == cudaSuccess &&
+            b->cell7.alloc(7 * (size_t)ncells, s) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     delete b;
@@ -167,8 +184,10 @@ extern "C" int mlipg_batch_create(mlipg_handle* h, int ncells, const int* natoms
                   cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(b->lat.p, lattices, 9 * (size_t)ncells * sizeof(double),
                   cudaMemcpyHostToDevice, s);
-  if (cudaStreamSynchronize(s) != cudaSuccess) {
-    cudaGetLastError();
+  // Copies from pageable memory are staged before cudaMemcpyAsync returns,
+  // so the host vectors may go; the batch's work stays queued on the stream
+  // behind whatever the stream already holds.
+  if (cudaGetLastError() != cudaSuccess) {
     delete b;
     return MLIPG_ECUDA;
   }
@@ -189,10 +208,20 @@ extern "C" int mlipg_batch_launch(mlipg_batch* b) {
   return cudaGetLastError() == cudaSuccess ? MLIPG_OK : MLIPG_ECUDA;
 }
 
+extern "C" int mlipg_batch_results(mlipg_batch* b, double* energies, double* forces,
+                                   double* virials);
+
 extern "C" int mlipg_batch_compute(mlipg_batch* b, double* energies, double* forces,
                                    double* virials) {
   int rc = mlipg_batch_launch(b);
   if (rc != MLIPG_OK) return rc;
+  return mlipg_batch_results(b, energies, forces, virials);
+}
+
+// Copies the results of a finished (or queued) launch back to the host.
+extern "C" int mlipg_batch_results(mlipg_batch* b, double* energies, double* forces,
+                                   double* virials) {
+  if (!b) return MLIPG_EINVAL;
   if (forces &&
       cudaMemcpyAsync(forces, b->f.p, 3 * (size_t)b->natoms * sizeof(double),
                       cudaMemcpyDeviceToHost, b->s) != cudaSuccess)
@@ -207,6 +236,20 @@ extern "C" int mlipg_batch_compute(mlipg_batch* b, double* energies, double* for
       for (int k = 0; k < 6; ++k) virials[6 * (size_t)c + k] = b->h_cell7[7 * (size_t)c + 1 + k];
   }
   return MLIPG_OK;
+}
+
+extern "C" int mlipg_batch_autotune(mlipg_batch* b, int max_report, double* report,
+                                    int* nreport) {
+  if (!b) return MLIPG_EINVAL;
+  return mlipg_autotune(b->h, b->natoms, b->x4.p, b->centers.p, b->off.p, b->idx.p, b->img.p,
+                        b->lat.p, b->ccell.p, b->nb_cap, b->f.p, b->out8.p, max_report, report,
+                        nreport);
+}
+
+extern "C" size_t mlipg_batch_device_bytes(const mlipg_batch* b) {
+  if (!b) return 0;
+  return (size_t)b->natoms * (sizeof(double4) + 4 + 4 + 4 + 24 + 8 + 48) +
+         (size_t)b->ncells * (9 * 8 + 4 + 56) + (size_t)b->npairs * 8;
 }
 
 extern "C" int mlipg_batch_sizes(const mlipg_batch* b, int* natoms, long long* npairs) {

@@ -88,6 +88,7 @@ struct mlipg_handle {
   DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_vatom, d_partials, d_status, d_out8;
   HostBuf h_x4, h_centers, h_off, h_idx, h_f, h_eatom, h_out;
   int last_status = 0;
+  int tiling_gen = 0;   // bumped whenever the schedules on the device change
   // per-launch timing of the fused kernel (measurement support)
   bool profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
@@ -327,6 +328,7 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
                 smem);
   int bps = fused_max_blocks_per_sm(fp64, M.L, smem);
   if (bps < 1) return fail(h, MLIPG_ENOTSUP, "fused kernel cannot be resident (smem %zu)", smem);
+  if (M.tiling.ctas_per_sm > 0) bps = std::min(bps, M.tiling.ctas_per_sm);
   int grid = std::max(1, std::min(ncenters, bps * h->num_sms));
   CK(h->d_partials.reserve((size_t)grid * 8 * sizeof(double)), "alloc partials");
   CK(h->d_status.reserve(sizeof(int)), "alloc status");
@@ -640,6 +642,102 @@ extern "C" double mlipg_flops_per_atom_step(const mlipg_handle* h, int elem, dou
 }
 
 
+// ------------------------------------------------------------------ tiling
+
+int mlipg_internal_tiling_generation(const mlipg_handle* h) { return h ? h->tiling_gen : 0; }
+
+extern "C" int mlipg_set_tiling(mlipg_handle* h, int irr_chunk, int warp_order,
+                                int ctas_per_sm) {
+  if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
+  Model& M = h->model;
+  const Tiling old = M.tiling;
+  M.tiling = Tiling{irr_chunk, warp_order, ctas_per_sm};
+  std::string err;
+  if (!build_schedules(M, err)) {
+    M.tiling = old;
+    std::string e2;
+    build_schedules(M, e2);
+    return fail(h, MLIPG_EINVAL, "mlipg_set_tiling(%d, %d, %d): %s", irr_chunk, warp_order,
+                ctas_per_sm, err.c_str());
+  }
+  h->tiling_gen++;
+  if (h->device < 0) return MLIPG_OK;
+  // the previous schedules may still be read by queued launches
+  CK(cudaStreamSynchronize(h->stream), "tiling: drain stream");
+  return upload_model(h);
+}
+
+extern "C" int mlipg_get_tiling(const mlipg_handle* h, int* out3) {
+  if (!h || !out3) return MLIPG_EINVAL;
+  out3[0] = h->model.tiling.irr_chunk;
+  out3[1] = h->model.tiling.warp_order;
+  out3[2] = h->model.tiling.ctas_per_sm;
+  return MLIPG_OK;
+}
+
+extern "C" int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4,
+                              const int* d_centers, const int* d_nbr_off, const int* d_nbr_idx,
+                              const int* d_img, const double* d_cell, const int* d_center_cell,
+                              int nb_cap, double* d_f, double* d_out8, int max_report,
+                              double* report, int* nreport) {
+  if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
+  if (h->device < 0) return fail(h, MLIPG_ENOGPU, "no CUDA device is available");
+  if (ncenters <= 0 || !d_x4 || !d_centers || !d_nbr_off || !d_nbr_idx || !d_f || !d_out8)
+    return fail(h, MLIPG_EINVAL, "mlipg_autotune: invalid arguments");
+  const Model& M = h->model;
+  const bool fp64 = h->precision == MLIPG_PREC_FP64;
+  const int cap = std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
+  const size_t smem = fused_smem_bytes(fp64, M.T, M.Lh, cap, std::max(M.max_nl, 1));
+  const int bps_max = std::max(1, fused_max_blocks_per_sm(fp64, M.L, smem));
+  // a sample of 16 centres per resident CTA keeps each candidate short
+  const int sample = std::min(ncenters, 16 * bps_max * h->num_sms);
+  const Tiling start = M.tiling;
+  struct Row { int chunk, order, cps; float ms; };
+  std::vector<Row> rows;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0), "event create");
+  CK(cudaEventCreate(&e1), "event create");
+  int rc = MLIPG_OK;
+  for (int chunk : {12, 24, 48})
+    for (int order : {0, 1})
+      for (int cps = 1; cps <= bps_max && rc == MLIPG_OK; ++cps) {
+        rc = mlipg_set_tiling(h, chunk, order, cps);
+        if (rc != MLIPG_OK) break;
+        float best = 1e30f;
+        for (int rep = 0; rep < 3 && rc == MLIPG_OK; ++rep) {
+          cudaEventRecord(e0, h->stream);
+          rc = run_kernel(h, sample, static_cast<const double4*>(d_x4), d_centers, d_nbr_off,
+                          d_nbr_idx, d_img, d_cell, d_center_cell, nullptr, nb_cap, d_f,
+                          nullptr, nullptr, d_out8);
+          cudaEventRecord(e1, h->stream);
+          if (rc == MLIPG_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = MLIPG_ECUDA;
+          float ms = 0;
+          if (rc == MLIPG_OK && rep > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
+            best = std::min(best, ms);
+        }
+        rows.push_back({chunk, order, cps, best});
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != MLIPG_OK) {
+    mlipg_set_tiling(h, start.irr_chunk, start.warp_order, start.ctas_per_sm);
+    return rc;
+  }
+  const Row* best = &rows[0];
+  for (const Row& r : rows)
+    if (r.ms < best->ms) best = &r;
+  const Row pick = *best;
+  if (report)
+    for (int k = 0; k < (int)rows.size() && k < max_report; ++k) {
+      report[4 * k + 0] = rows[k].chunk;
+      report[4 * k + 1] = rows[k].order;
+      report[4 * k + 2] = rows[k].cps;
+      report[4 * k + 3] = rows[k].ms;
+    }
+  if (nreport) *nreport = (int)rows.size();
+  return mlipg_set_tiling(h, pick.chunk, pick.order, pick.cps);
+}
+
 // Support of the allocation-free entry point (noalloc.cu): the same launch as
 // run_kernel, with the partial-sum and status scratch supplied by the caller
 // and without touching any grow-only buffer (nothing is allocated here).
@@ -667,8 +765,9 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
   const size_t smem = fused_smem_bytes(fp64, M.T, M.Lh, nb_cap, nl_cap);
   if (smem > 227 * 1024)
     return fail(h, MLIPG_ENOTSUP, "model needs %zu bytes of shared memory per CTA", smem);
-  const int bps = fused_max_blocks_per_sm(fp64, M.L, smem);
+  int bps = fused_max_blocks_per_sm(fp64, M.L, smem);
   if (bps < 1) return fail(h, MLIPG_ENOTSUP, "fused kernel cannot be resident (smem %zu)", smem);
+  if (M.tiling.ctas_per_sm > 0) bps = std::min(bps, M.tiling.ctas_per_sm);
   const int grid = std::max(1, std::min(ncenters, bps * h->num_sms));
   if (grid > partial_slots)
     return fail(h, MLIPG_ECAPACITY,

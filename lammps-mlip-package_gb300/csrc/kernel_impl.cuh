@@ -772,6 +772,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       const R* wl = wlin_table(A);
       for (int u = warp; u < nI; u += kBlock / 32) {
         const DeviceIrrUnit iu = A.iunits[i0 + u];
+        if (iu.nterm == 0) continue;   // padding of a balanced schedule
         if (T == 3)
           dispatch_irr<3>(iu, A.tuples, A.terms, wl, hnl, sa, sg, Lh, n, half, act, eacc);
         else if (T == 2)
@@ -781,6 +782,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       }
       for (int u = warp; u < nU; u += kBlock / 32) {
         const DeviceUnit un = A.units[u0 + u];
+        if (un.nterm == 0) continue;
         double hv = 0.0;
         if (act) {
           hv = __ldg(A.w_lin + (size_t)un.itc * kNPad + n);

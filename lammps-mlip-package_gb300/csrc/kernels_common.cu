@@ -4,6 +4,7 @@
 namespace mlipg {
 
 static_assert(sizeof(DeviceTerm) == 16, "DeviceTerm must be 16 bytes");
+static_assert(kBlock / 32 == kCtaWarps, "schedules are dealt to the CTA's warps");
 static_assert(sizeof(DeviceUnit) == 32, "DeviceUnit must be 32 bytes");
 static_assert(sizeof(DevicePoly) == 32, "DevicePoly must be 32 bytes");
 

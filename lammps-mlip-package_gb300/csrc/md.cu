@@ -20,6 +20,10 @@
 
 #include "../../include/mlipg.h"
 
+// Changes whenever the handle's work schedules are rebuilt (autotuning):
+// a captured step holds their device addresses and launch shape.
+int mlipg_internal_tiling_generation(const mlipg_handle* h);
+
 namespace {
 
 constexpr double kFtm2v = 1.0 / 1.0364269e-4;  // metal units
@@ -119,6 +123,7 @@ struct mlipg_md {
   DBuf<int> centers, off, idx, img, ccell, flag;
   cudaGraphExec_t graph = nullptr;
   double graph_dt = 0;
+  int graph_tiling = 0;   // schedule generation the graph was captured with
   int* hflag = nullptr;
   std::vector<double> hx;
 };
@@ -263,7 +268,8 @@ extern "C" int mlipg_md_create(mlipg_handle* h, const double* lattice9, int nato
 
 extern "C" int mlipg_md_run(mlipg_md* md, int nsteps, double dt, int use_graph) {
   if (!md || nsteps < 0 || !(dt > 0)) return MLIPG_EINVAL;
-  if (md->graph && md->graph_dt != dt) {
+  if (md->graph &&
+      (md->graph_dt != dt || md->graph_tiling != mlipg_internal_tiling_generation(md->h))) {
     cudaGraphExecDestroy(md->graph);
     md->graph = nullptr;
   }
@@ -308,6 +314,7 @@ extern "C" int mlipg_md_run(mlipg_md* md, int nsteps, double dt, int use_graph) 
       cudaGraphDestroy(g);
       MCK(e);
       md->graph_dt = dt;
+      md->graph_tiling = mlipg_internal_tiling_generation(md->h);
     }
   }
   MCK(cudaStreamSynchronize(md->s));

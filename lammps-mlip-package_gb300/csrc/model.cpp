@@ -301,7 +301,30 @@ bool fold_terms(Model& M, std::string& err) {
   return true;
 }
 
-bool build_schedules(Model& M, std::string& err) {
+// Deals cost-sorted work items to kCtaWarps lists, each item onto the
+// least-loaded list (longest processing time first), and interleaves the
+// lists so that the kernel's round-robin `for (u = warp; ...; u += kCtaWarps)`
+// walks exactly list `warp`; short lists are padded with `pad`.
+template <typename U, typename Cost>
+std::vector<U> deal_longest_first(std::vector<U> v, Cost cost, double* load, const U& pad) {
+  std::stable_sort(v.begin(), v.end(), [&](const U& a, const U& b) { return cost(a) > cost(b); });
+  std::vector<std::vector<U>> lists(kCtaWarps);
+  for (const U& x : v) {
+    int w = 0;
+    for (int k = 1; k < kCtaWarps; ++k)
+      if (load[k] < load[w]) w = k;
+    lists[w].push_back(x);
+    load[w] += cost(x);
+  }
+  size_t rounds = 0;
+  for (auto& l : lists) rounds = std::max(rounds, l.size());
+  std::vector<U> out(rounds * kCtaWarps, pad);
+  for (int w = 0; w < kCtaWarps; ++w)
+    for (size_t r = 0; r < lists[w].size(); ++r) out[r * kCtaWarps + w] = lists[w][r];
+  return out;
+}
+
+bool schedules_for_tiling(Model& M, std::string& err) {
   const int T = M.T, F = M.F;
   // nonlinear itc: appear in any polynomial term of order >= 2
   std::vector<char> is_nl(M.n_itc, 0);
@@ -368,10 +391,10 @@ bool build_schedules(Model& M, std::string& err) {
         const bool fix0 = (q == 3 && T == 3);
         const int nsub = fix0 ? T : 1;
         for (int s0 = 0; s0 < nsub; ++s0)
-          for (int c0 = 0; c0 < M.irr_cnterms[k]; c0 += kIrrChunk) {
+          for (int c0 = 0; c0 < M.irr_cnterms[k]; c0 += M.tiling.irr_chunk) {
             DeviceIrrUnit iu{};
             iu.term0 = M.irr_cfirst[k] + c0;
-            iu.nterm = std::min(kIrrChunk, M.irr_cnterms[k] - c0);
+            iu.nterm = std::min(M.tiling.irr_chunk, M.irr_cnterms[k] - c0);
             iu.tup = tup0 + (fix0 ? s0 * T * T : 0);
             iu.q = (uint8_t)q;
             iu.s0 = (uint8_t)s0;
@@ -426,11 +449,38 @@ bool build_schedules(Model& M, std::string& err) {
         err = "internal error: work schedule does not cover every feature once";
         return false;
       }
+    if (M.tiling.warp_order == 1) {
+      // per-warp cost ~ terms x tuples x order (products and adjoint products)
+      const auto icost = [&](const DeviceIrrUnit& u) {
+        int nt = 1;
+        for (int p = 0; p < u.q; ++p) nt *= T;
+        if (u.q == 3 && T == 3) nt /= T;
+        return (double)u.nterm * nt * u.q;
+      };
+      const auto ucost = [](const DeviceUnit& u) { return (double)u.nterm * u.q; };
+      double load[kCtaWarps] = {};
+      DeviceIrrUnit ipad{};
+      ipad.tup = S.iunits.empty() ? 0 : S.iunits[0].tup;
+      DeviceUnit upad{};
+      upad.itc = -1;
+      upad.nl_slot = -1;
+      S.iunits = deal_longest_first(S.iunits, icost, load, ipad);
+      S.units = deal_longest_first(S.units, ucost, load, upad);
+    }
   }
   return true;
 }
 
 }  // namespace
+
+bool build_schedules(Model& M, std::string& err) {
+  if (M.tiling.irr_chunk < 2 || M.tiling.irr_chunk > 4096 || M.tiling.irr_chunk % 2 ||
+      M.tiling.warp_order < 0 || M.tiling.warp_order > 1 || M.tiling.ctas_per_sm < 0) {
+    err = "invalid tiling";
+    return false;
+  }
+  return schedules_for_tiling(M, err);
+}
 
 bool read_potential(const std::string& path, Potential& p, std::string& err) {
   std::ifstream in(path);
@@ -587,7 +637,7 @@ bool build_model(Model& M, std::string& err) {
     M.other_type[tc * M.T + tpm[tc].second] = tpm[tc].first;
   }
   if (!fold_terms(M, err)) return false;
-  return build_schedules(M, err);
+  return schedules_for_tiling(M, err);
 }
 
 bool count_coefficients(int n_types, int model_type, int maxp, int maxl, int gtinv_order,

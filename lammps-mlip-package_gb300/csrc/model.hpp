@@ -84,7 +84,19 @@ struct DeviceTuple {      // 8 bytes
   int itc;                // -1: not a feature (non-canonical ordering)
   int nl_slot;            // slot among nonlinear features, -1 if linear only
 };
-constexpr int kIrrChunk = 24;  // canonical terms per batched unit
+constexpr int kIrrChunk = 24;  // default canonical terms per batched unit
+constexpr int kCtaWarps = 8;   // warps of the fused kernel's CTA (units are dealt to them)
+
+// Tile shape of the fused kernel's invariant/adjoint phase, chosen by the
+// autotuner: terms per batched unit, the order in which units are dealt to
+// the CTA's warps (0 = cost-sorted round robin, 1 = longest-first onto the
+// least-loaded warp, padded with empty units), and CTAs per SM of the
+// persistent grid (0 = as many as are resident).
+struct Tiling {
+  int irr_chunk = kIrrChunk;
+  int warp_order = 0;
+  int ctas_per_sm = 0;
+};
 
 struct ITC {
   int irreps;
@@ -117,6 +129,7 @@ struct Model {
   std::vector<int> type_pairs;                // [T*T] -> tc
   std::vector<int> other_type;                // [TC*T]
   std::vector<Schedule> sched;                // [T]
+  Tiling tiling;
   int max_nl = 0;                             // max nonlinear itc over elements
 };
 
@@ -125,6 +138,9 @@ bool read_potential(const std::string& path, Potential& p, std::string& err);
 
 // Builds the complete model (table screening, enumeration, schedules).
 bool build_model(Model& m, std::string& err);
+
+// Rebuilds the per-element work schedules for m.tiling.
+bool build_schedules(Model& m, std::string& err);
 
 // Counts coefficients and features for a model specification.
 bool count_coefficients(int n_types, int model_type, int maxp, int maxl, int gtinv_order,

@@ -81,7 +81,18 @@ def lib():
         "mlipg_batch_compute": (i32, [P, dp, dp, dp]),
         "mlipg_batch_sizes": (i32, [P, ip, llp]),
         "mlipg_batch_destroy": (None, [P]),
+        "mlipg_batch_results": (i32, [P, dp, dp, dp]),
+        "mlipg_batch_device_bytes": (ctypes.c_size_t, [P]),
+        "mlipg_server_create": (i32, [ctypes.c_char_p, ctypes.c_size_t, i32, ctypes.POINTER(P)]),
+        "mlipg_server_submit": (i32, [P, i32, dp, dp, ip, i32, llp]),
+        "mlipg_server_wait": (i32, [P, ctypes.c_longlong, i32, dp, dp, dp]),
+        "mlipg_server_stats": (i32, [P, dp]),
+        "mlipg_server_destroy": (None, [P]),
         "mlipg_measure_fma_peak": (i32, [i32, dp]),
+        "mlipg_set_tiling": (i32, [P, i32, i32, i32]),
+        "mlipg_get_tiling": (i32, [P, ip]),
+        "mlipg_autotune": (i32, [P, i32, P, P, P, P, P, P, P, i32, P, P, i32, dp, ip]),
+        "mlipg_batch_autotune": (i32, [P, i32, dp, ip]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -189,6 +200,24 @@ class Potential:
 
     def stream(self) -> int:
         return lib().mlipg_stream(self.h) or 0
+
+    def set_tiling(self, irr_chunk: int = 24, warp_order: int = 0, ctas_per_sm: int = 0):
+        _check(lib().mlipg_set_tiling(self.h, irr_chunk, warp_order, ctas_per_sm), self.h)
+
+    def tiling(self):
+        o = (ctypes.c_int * 3)()
+        _check(lib().mlipg_get_tiling(self.h, o), self.h)
+        return {"irr_chunk": o[0], "warp_order": o[1], "ctas_per_sm": o[2]}
+
+    def autotune_device(self, ncenters, x4, centers, nbr_off, nbr_idx, f, out8, img=0, cell=0,
+                        center_cell=0, nb_cap=0):
+        """Autotunes on device buffers (pointers, as for compute_device)."""
+        rep = np.zeros(4 * 64)
+        n = ctypes.c_int()
+        _check(lib().mlipg_autotune(self.h, ncenters, x4, centers, nbr_off, nbr_idx,
+                                    img or None, cell or None, center_cell or None, nb_cap, f,
+                                    out8, 64, _dp(rep), ctypes.byref(n)), self.h)
+        return _tiling_rows(rep, n.value)
 
     def itc_list(self):
         n = lib().mlipg_dump_itc(self.h, None, 0)
@@ -341,6 +370,12 @@ def maxwell_boltzmann(masses, temperature, rng):
     return v * np.sqrt(temperature / t) if t > 0 else v
 
 
+def _tiling_rows(rep, n):
+    r = rep.reshape(-1, 4)[:min(n, 64)]
+    return [{"irr_chunk": int(a), "warp_order": int(b), "ctas_per_sm": int(c), "ms": float(d)}
+            for a, b, c, d in r]
+
+
 class Batch:
     """Many periodic cells evaluated in one persistent launch (see mlipg_batch_*)."""
 
@@ -367,6 +402,13 @@ class Batch:
     def launch(self):
         _check(lib().mlipg_batch_launch(self.h))
 
+    def autotune(self):
+        """Picks the potential's tile shape for this batch; returns the timing table."""
+        rep = np.zeros(4 * 64)
+        n = ctypes.c_int()
+        _check(lib().mlipg_batch_autotune(self.h, 64, _dp(rep), ctypes.byref(n)), self.pot.h)
+        return _tiling_rows(rep, n.value)
+
     def compute(self):
         e = np.zeros(self.ncells)
         f = np.zeros((self.total_atoms, 3))
@@ -379,6 +421,55 @@ class Batch:
     def close(self):
         if getattr(self, "h", None):
             lib().mlipg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Server:
+    """Continuous-batching request loop (see mlipg_server_*)."""
+
+    STATS = ["completed", "p50_ms", "p99_ms", "atom_steps_per_s", "batches", "device_bytes",
+             "queued", "in_flight"]
+
+    def __init__(self, path: str, budget_bytes: int = 64 << 30, max_batch_atoms: int = 65536):
+        lib()
+        h = ctypes.c_void_p()
+        _check(lib().mlipg_server_create(os.fsencode(path), budget_bytes, max_batch_atoms,
+                                         ctypes.byref(h)))
+        self.h = h
+        self.natoms = {}
+
+    def submit(self, cell, precision: int) -> int:
+        lat = np.ascontiguousarray(cell.lattice, dtype=np.float64)
+        x = np.ascontiguousarray(cell.positions, dtype=np.float64)
+        t = np.ascontiguousarray(cell.types, dtype=np.int32)
+        tk = ctypes.c_longlong()
+        _check(lib().mlipg_server_submit(self.h, cell.natoms, _dp(lat), _dp(x), _ip(t),
+                                         precision, ctypes.byref(tk)))
+        self.natoms[tk.value] = cell.natoms
+        return tk.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000):
+        n = self.natoms.get(ticket, 0)
+        e = ctypes.c_double()
+        f = np.zeros((n, 3))
+        v = np.zeros(6)
+        rc = lib().mlipg_server_wait(self.h, ticket, timeout_ms, ctypes.byref(e), _dp(f), _dp(v))
+        if rc != 0:
+            raise MlipgError(rc, "mlipg_server_wait")
+        del self.natoms[ticket]
+        return e.value, f, v
+
+    def stats(self):
+        o = np.zeros(8)
+        _check(lib().mlipg_server_stats(self.h, _dp(o)))
+        return dict(zip(self.STATS, o.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mlipg_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

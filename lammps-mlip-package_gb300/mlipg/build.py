@@ -47,6 +47,7 @@ def _sources():
         "model.o": ("g++", os.path.join(CSRC, "model.cpp")),
         "capi.o": ("g++", os.path.join(CSRC, "capi.cpp")),
         "neighbor.o": ("g++", os.path.join(CSRC, "neighbor.cpp")),
+        "serve.o": ("g++", os.path.join(CSRC, "serve.cpp")),
         "kernels_common.o": ("nvcc", os.path.join(CSRC, "kernels_common.cu")),
         "peak.o": ("nvcc", os.path.join(CSRC, "peak.cu")),
         "noalloc.o": ("nvcc", os.path.join(CSRC, "noalloc.cu")),

@@ -209,6 +209,9 @@ def random_triclinic_cell(natoms: int, density: float, ntypes: int,
         break
     frac = rng.random((natoms, 3))
     md2 = min_dist * min_dist
+    if natoms > 512:
+        return Cell(lat, _place_kdtree(frac, lat, min_dist, rng, max_rounds) @ lat,
+                    np.asarray(rng.integers(0, ntypes, natoms), dtype=np.int32))
 
     def min_r2(ids):
         d = frac[ids][:, None, :] - frac[None, :, :]
@@ -229,6 +232,64 @@ def random_triclinic_cell(natoms: int, density: float, ntypes: int,
         raise RuntimeError("could not place atoms with the minimum distance")
     types = np.asarray(rng.integers(0, ntypes, natoms), dtype=np.int32)
     return Cell(lat, frac @ lat, types)
+
+
+def _place_kdtree(frac, lat, min_dist, rng, max_rounds):
+    """Minimum-distance rejection for large cells with k-d trees over atoms
+    and their 26 neighbouring images (every cell width exceeds `min_dist`).
+    Atoms closer than `min_dist` to an earlier atom are redrawn; each redraw
+    round tries 16 candidate positions per atom against the placed atoms and
+    keeps the first free one that also clears the atoms placed before it in
+    the same round."""
+    import itertools
+
+    from scipy.spatial import cKDTree
+
+    n = frac.shape[0]
+    img = np.array(list(itertools.product((-1, 0, 1), repeat=3)), dtype=np.float64) @ lat
+
+    def tree_of(f):
+        pos = f @ lat
+        return cKDTree((pos[None, :, :] + img[:, None, :]).reshape(-1, 3))
+
+    def earlier_clash(f):
+        """Indices (into f) of points within min_dist of an earlier point."""
+        m = f.shape[0]
+        pos = f @ lat
+        tree = tree_of(f)
+        cnt = tree.query_ball_point(pos, min_dist, return_length=True)
+        near = np.nonzero(cnt > 1)[0]
+        hits = tree.query_ball_point(pos[near], min_dist) if near.size else []
+        return np.asarray([i for i, h in zip(near, hits) if (np.asarray(h) % m).min() < i],
+                          dtype=np.int64)
+
+    bad = earlier_clash(frac)
+    keep = np.ones(n, dtype=bool)
+    keep[bad] = False
+    tree = tree_of(frac[keep])
+    extra = np.zeros((0, 3))
+    for _ in range(max_rounds):
+        if bad.size == 0:
+            return frac
+        cand = rng.random((bad.size, 16, 3))
+        flat = (cand @ lat).reshape(-1, 3)
+        free = tree.query(flat, k=1, distance_upper_bound=min_dist)[0] > min_dist
+        if extra.shape[0]:
+            free &= tree_of(extra).query(flat, k=1, distance_upper_bound=min_dist)[0] > min_dist
+        free = free.reshape(bad.size, 16)
+        has = free.any(axis=1)
+        placed = bad[has]
+        newf = cand[has, np.argmax(free[has], axis=1)]
+        clash = np.zeros(placed.size, dtype=bool)
+        clash[earlier_clash(newf)] = True
+        frac[placed[~clash]] = newf[~clash]
+        keep[placed[~clash]] = True
+        bad = np.concatenate([bad[~has], placed[clash]])
+        extra = np.concatenate([extra, newf[~clash]])
+        if extra.shape[0] > 1024:
+            tree = tree_of(frac[keep])
+            extra = np.zeros((0, 3))
+    raise RuntimeError("could not place atoms with the minimum distance")
 
 
 def read_lammps_data(path: str) -> Cell:

@@ -89,3 +89,24 @@ def test_compute_without_gpu_fails_loudly(potdir):
     with pytest.raises(mlipg.MlipgError) as e:
         p.compute_lammps(1, 1, np.zeros((1, 3)), [1], [0], [0], [np.zeros(0, np.int32)])
     assert e.value.code == 7
+
+
+def test_tiling_candidates_build_on_host(tmp_path):
+    """Every autotuner candidate builds a schedule that covers each feature once
+    (the library checks coverage and fails otherwise); invalid shapes are
+    rejected and leave the previous tiling in place."""
+    import mlipg
+    from mlipg.potential import workload_potential
+    for name in ("fcc-ternary-1m", "triclinic-batch", "fcc-al-256"):
+        p = str(tmp_path / (name + ".mlip"))
+        workload_potential(p, name)
+        g = mlipg.Potential(p, mlipg.PREC_MIXED)
+        for chunk in (12, 24, 48):
+            for order in (0, 1):
+                g.set_tiling(chunk, order, 1)
+                assert g.tiling() == {"irr_chunk": chunk, "warp_order": order, "ctas_per_sm": 1}
+        for bad in ((13, 0, 0), (24, 2, 0), (24, 0, -1), (0, 0, 0)):
+            with pytest.raises(mlipg.MlipgError):
+                g.set_tiling(*bad)
+        assert g.tiling()["irr_chunk"] == 48
+        g.close()
