@@ -282,6 +282,15 @@ def run_ours(args, dist):
     torch.cuda.synchronize()
 
     ncent_main = min(natoms, args.centres) if args.centres > 0 else natoms
+    tune = None
+    if args.tiling:
+        g.set_tiling(*[int(v) for v in args.tiling.split(",")])
+        tune = {"table": None, "picked": g.tiling()}
+    if args.autotune:
+        tune = {"table": g.autotune_device(natoms, d_x4.data_ptr(), d_cent.data_ptr(),
+                                           d_off.data_ptr(), d_idx.data_ptr(), d_f.data_ptr(),
+                                           d_out.data_ptr(), nb_cap=nb_cap),
+                "picked": g.tiling()}
 
     def step(ncent=None):
         ncent = ncent_main if ncent is None else ncent
@@ -439,7 +448,8 @@ def run_ours(args, dist):
                                              % (SKIN, sysm.npairs, sysm.npairs * 4 / 1e6),
                            "l2": "inputs larger than L2 (positions + neighbour list %.0f MB)"
                                  % ((32 * sysm.nall + 4 * sysm.npairs) / 1e6),
-                           "step": "energy + forces + virial of all atoms, one fused launch"},
+                           "step": "energy + forces + virial of all atoms, one fused launch",
+                           "tiling": tune},
                 "e2e": e2e,
                 "fp64": {"value": fp64_v, "unit": UNIT, "centres": nsub,
                          "mixed_over_fp64": value / dist["world"] / fp64_v},
@@ -506,7 +516,7 @@ def run_batch(args, dist):
     cpu = cpu_baseline_cells(pot, cells, args.cpu_seconds) \
         if rank == 0 and args.cpu_seconds > 0 else None
     dev = torch.device("cuda", 0)
-    res, rates, kms, create_s = {}, {}, {}, {}
+    res, rates, kms, create_s, tune = {}, {}, {}, {}, {}
     clk = None
     for prec in (mlipg.PREC_FP64, mlipg.PREC_MIXED):
         g = mlipg.Potential(pot, prec)
@@ -514,6 +524,7 @@ def run_batch(args, dist):
         t0 = time.perf_counter()
         b = mlipg.Batch(g, cells)
         create_s[prec] = time.perf_counter() - t0
+        tune[prec] = {"table": b.autotune(), "picked": g.tiling()} if args.autotune else None
         for _ in range(args.warmup):
             b.launch()
         torch.cuda.synchronize()
@@ -585,7 +596,9 @@ def run_batch(args, dist):
                            "potential": POT_DESC[spec["pot"]],
                            "neighbours_per_atom": npairs / natoms,
                            "l2": "inputs larger than L2 (%.0f MB)" % (h2d / 1e6),
-                           "step": "one persistent launch over all cells + per-cell sums"},
+                           "step": "one persistent launch over all cells + per-cell sums",
+                           "tiling": {"mixed": tune[mlipg.PREC_MIXED],
+                                      "fp64": tune[mlipg.PREC_FP64]}},
                 "fp64": {"value": rates[mlipg.PREC_FP64], "unit": UNIT,
                          "kernel_ms": kms[mlipg.PREC_FP64],
                          "mixed_over_fp64": rates[mlipg.PREC_MIXED] / rates[mlipg.PREC_FP64]},
@@ -778,7 +791,13 @@ def main():
     ap.add_argument("--pool", type=int, default=256,
                     help="serving: distinct structures the requests are drawn from")
     ap.add_argument("--max-batch-atoms", type=int, default=65536)
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default tile shape instead of autotuning it")
+    ap.add_argument("--tiling", default="",
+                    help="fixed tile shape 'terms,order,ctas_per_sm' (implies --no-autotune)")
     args = ap.parse_args()
+    if args.tiling:
+        args.autotune = False
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = {"world": world, "rank": rank}

@@ -195,6 +195,28 @@ int mlipg_batch_sizes(const mlipg_batch* b, int* natoms, long long* npairs);
 int mlipg_batch_autotune(mlipg_batch* b, int max_report, double* report, int* nreport);
 void mlipg_batch_destroy(mlipg_batch* b);
 
+/* Device neighbour lists for one or many periodic cells (no ghost atoms).
+ * mlipg_dnlist_build wraps d_x4 (double4 x, y, z, element; cells stored one
+ * after another, natoms[c] atoms each, lattice rows a1 a2 a3 per cell) into
+ * its cells IN PLACE and builds full lists within rlist with packed image
+ * codes ((n1+512) | (n2+512) << 10 | (n3+512) << 20, 0 for no shift): the
+ * neighbour of i at entry p is x[idx[p]] + n1 a1 + n2 a2 + n3 a3.  Lists are
+ * in a deterministic order (stencil bins, then atom index).  Pair arrays grow
+ * with headroom_pct percent spare; mlipg_dnlist_arrays reports the device
+ * arrays (CSR offsets, indices, image codes, cell of each atom, lattices),
+ * the pair count, the longest list and a generation number that changes
+ * whenever an array moved.  The reference builds its (half, displacement)
+ * lists on the host: src/USER-MLIP/mlipkk_cell.cpp:218-307. */
+typedef struct mlipg_dnlist mlipg_dnlist;
+int mlipg_dnlist_create(void* cuda_stream, mlipg_dnlist** out);
+int mlipg_dnlist_build(mlipg_dnlist* L, int ncells, const int* natoms, const double* lattices,
+                       void* d_x4, double rlist, int headroom_pct);
+int mlipg_dnlist_arrays(const mlipg_dnlist* L, const int** d_off, const int** d_idx,
+                        const int** d_img, const int** d_center_cell, const double** d_cells,
+                        long long* npairs, int* max_neigh, int* generation);
+int mlipg_dnlist_copy(const mlipg_dnlist* L, int* off, int* idx, int* img);
+void mlipg_dnlist_destroy(mlipg_dnlist* L);
+
 /* Tile shape of the fused kernel and its autotuner.  No counterpart in the
  * reference (its Kokkos team sizes are fixed at compile time).
  * irr_chunk: coupling terms per batched work unit (even, 2..4096; default 24);

@@ -1,21 +1,21 @@
 // Many independent periodic cells evaluated in one persistent launch.
 //
-// Each cell's atoms are wrapped into its cell and get a full neighbour list
-// of owned atoms whose entries carry packed periodic image codes (no ghost
-// atoms; small cells see their own images).  All cells are concatenated:
-// one fused-kernel launch evaluates every centre of every cell (uneven cell
-// sizes balance across the persistent grid), then one block per cell sums
-// its per-atom energies and virials in a fixed order.  Energies (eV),
-// forces (eV/A, per atom) and the virial per cell (LAMMPS order xx yy zz xy
-// xz yz, -sum r_ij (x) f_ij) come back to the host.
+// The cells' atoms are uploaded once (positions + element as double4, the
+// lattices) and the device neighbour builder wraps them into their cells and
+// writes full lists of owned atoms whose entries carry packed periodic image
+// codes (no ghost atoms; small cells see their own images).  The lists are
+// built on the batch's own stream, so building one batch never waits for
+// the evaluations queued on the handle's stream.  One fused-kernel launch
+// evaluates every centre of every cell (uneven cell sizes balance across
+// the persistent grid), then one block per cell sums its per-atom energies
+// and virials in a fixed order.  Energies (eV), forces (eV/A, per atom) and
+// the virial per cell (LAMMPS order xx yy zz xy xz yz, -sum r_ij (x) f_ij)
+// come back to the host.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
 #include <vector>
-#ifdef _OPENMP
-#include <omp.h>
-#endif
 
 #include "../../include/mlipg.h"
 
@@ -40,9 +40,14 @@ __global__ void k_cell_sums(const int* __restrict__ off, const double* __restric
   if (threadIdx.x < 7) out7[7 * (size_t)c + threadIdx.x] = red[threadIdx.x][0];
 }
 
-// Stream-ordered device buffer: allocated and freed on the batch's stream
-// from the device's memory pool, so creating and retiring batches never
-// synchronises the device (other streams keep running).
+__global__ void k_iota(int n, int* __restrict__ v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = i;
+}
+
+// Stream-ordered device buffer: allocated and freed on the batch's build
+// stream from the device's memory pool, so creating and retiring batches
+// never synchronises the device (other streams keep running).
 template <typename T>
 struct Dev {
   T* p = nullptr;
@@ -60,17 +65,36 @@ struct Dev {
 
 struct mlipg_batch {
   mlipg_handle* h = nullptr;
-  cudaStream_t s = nullptr;
+  cudaStream_t s = nullptr;    // the handle's stream: evaluations
+  cudaStream_t bs = nullptr;   // this batch's stream: upload, lists, buffer lifetime
+  cudaEvent_t built = nullptr, done = nullptr;
   int ncells = 0;
   int natoms = 0;
   long long npairs = 0;
   int nb_cap = 0;
-  std::vector<int> cell_off;
+  mlipg_dnlist* nl = nullptr;
   Dev<double4> x4;
-  Dev<int> centers, off, idx, img, ccell, d_cell_off;
-  Dev<double> lat, f, eatom, vatom, out8, cell7;
+  Dev<int> centers, d_cell_off;
+  Dev<double> f, eatom, vatom, out8, cell7;
   std::vector<double> h_cell7;
+  ~mlipg_batch() {
+    // buffers are freed on bs once every evaluation queued on s has finished
+    if (done && s && bs && cudaEventRecord(done, s) == cudaSuccess) cudaStreamWaitEvent(bs, done, 0);
+    mlipg_dnlist_destroy(nl);
+    if (built) cudaEventDestroy(built);
+    if (done) cudaEventDestroy(done);
+  }
 };
+
+static void keep_pool_memory() {
+  // keep freed batch memory in the pool (a serving loop reuses it at once)
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    unsigned long long keep = ~0ULL;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+}
 
 extern "C" int mlipg_batch_create(mlipg_handle* h, int ncells, const int* natoms,
                                   const double* lattices, const double* x, const int* elements,
@@ -79,117 +103,69 @@ extern "C" int mlipg_batch_create(mlipg_handle* h, int ncells, const int* natoms
   *out = nullptr;
   cudaStream_t s = static_cast<cudaStream_t>(mlipg_stream(h));
   if (!s) return MLIPG_ENOGPU;
-  const double rc = mlipg_cutoff(h);
+  const int ne = mlipg_num_elements(h);
   std::vector<int> aoff(ncells + 1, 0);
   for (int c = 0; c < ncells; ++c) {
-    if (natoms[c] <= 0) return MLIPG_EINVAL;
+    if (natoms[c] <= 0 || aoff[c] > (1 << 30) - natoms[c]) return MLIPG_EINVAL;
     aoff[c + 1] = aoff[c] + natoms[c];
   }
   const int N = aoff[ncells];
-  // per-cell neighbour lists (image-coded, owner indices), built in parallel
-  std::vector<std::vector<int>> c_off(ncells), c_idx(ncells), c_img(ncells);
-  std::vector<std::vector<double>> c_x(ncells);
-  int err = MLIPG_OK;
-#pragma omp parallel for schedule(dynamic, 4)
-  for (int c = 0; c < ncells; ++c) {
-    mlipg_nlist* nl = nullptr;
-    const int n = natoms[c];
-    if (mlipg_nlist_build(lattices + 9 * (size_t)c, n, x + 3 * (size_t)aoff[c],
-                          elements + aoff[c], rc, &nl) != MLIPG_OK) {
-      err = MLIPG_EINVAL;
-      continue;
-    }
-    int nall = 0;
-    long long np = 0;
-    mlipg_nlist_sizes(nl, &nall, &np);
-    std::vector<double> xa((size_t)nall * 3);
-    std::vector<int> owner(nall), image(nall);
-    c_off[c].resize(n + 1);
-    c_idx[c].resize((size_t)np);
-    mlipg_nlist_copy(nl, xa.data(), nullptr, owner.data(), image.data(), c_off[c].data(),
-                     c_idx[c].data());
-    mlipg_nlist_destroy(nl);
-    c_img[c].resize((size_t)np);
-    for (long long p = 0; p < np; ++p) {
-      const int j = c_idx[c][p];
-      c_img[c][p] = image[j];
-      c_idx[c][p] = owner[j] + aoff[c];
-    }
-    xa.resize((size_t)n * 3);
-    c_x[c] = std::move(xa);
+  std::vector<double4> hx4(N);
+  for (int i = 0; i < N; ++i) {
+    if (elements[i] < 0 || elements[i] >= ne) return MLIPG_EINVAL;
+    hx4[i] = double4{x[3 * (size_t)i], x[3 * (size_t)i + 1], x[3 * (size_t)i + 2],
+                     (double)elements[i]};
   }
-  if (err != MLIPG_OK) return err;
-  {
-    // keep freed batch memory in the pool (a serving loop reuses it at once)
-    int dev = 0;
-    cudaMemPool_t pool;
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-      unsigned long long keep = ~0ULL;
-      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-    }
-  }
+  keep_pool_memory();
   mlipg_batch* b = new mlipg_batch();
   b->h = h;
   b->s = s;
   b->ncells = ncells;
   b->natoms = N;
-  b->cell_off = aoff;
-  std::vector<long long> poff(ncells + 1, 0);
-  for (int c = 0; c < ncells; ++c) poff[c + 1] = poff[c] + (long long)c_idx[c].size();
-  b->npairs = poff[ncells];
-  if (b->npairs > 2147483647LL) {
-    delete b;
-    return MLIPG_EINVAL;
+  if (cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->built, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    mlipg_batch_destroy(b);
+    return MLIPG_ECUDA;
   }
-  std::vector<double4> hx4(N);
-  std::vector<int> hcent(N), hoff(N + 1), hcc(N), hidx((size_t)b->npairs), himg((size_t)b->npairs);
-  int maxn = 0;
-#pragma omp parallel for schedule(dynamic, 4) reduction(max : maxn)
-  for (int c = 0; c < ncells; ++c) {
-    for (int i = 0; i < natoms[c]; ++i) {
-      const int g = aoff[c] + i;
-      hx4[g] = double4{c_x[c][3 * i], c_x[c][3 * i + 1], c_x[c][3 * i + 2],
-                       (double)elements[g]};
-      hcent[g] = g;
-      hcc[g] = c;
-      hoff[g] = (int)(poff[c] + c_off[c][i]);
-      maxn = std::max(maxn, c_off[c][i + 1] - c_off[c][i]);
-    }
-    std::memcpy(hidx.data() + poff[c], c_idx[c].data(), c_idx[c].size() * sizeof(int));
-    std::memcpy(himg.data() + poff[c], c_img[c].data(), c_img[c].size() * sizeof(int));
-  }
-  hoff[N] = (int)b->npairs;
-  b->nb_cap = maxn;
-  bool ok = b->x4.alloc(N, s) == cudaSuccess && b->centers.alloc(N, s) == cudaSuccess &&
-            b->off.alloc(N + 1, s) == cudaSuccess && b->idx.alloc(b->npairs, s) == cudaSuccess &&
-            b->img.alloc(b->npairs, s) == cudaSuccess && b->ccell.alloc(N, s) == cudaSuccess &&
-            b->d_cell_off.alloc(ncells + 1, s) == cudaSuccess &&
-            b->lat.alloc(9 * (size_t)ncells, s) == cudaSuccess &&
-            b->f.alloc(3 * (size_t)N, s) == cudaSuccess && b->eatom.alloc(N, s) == cudaSuccess &&
-            b->vatom.alloc(6 * (size_t)N, s) == cudaSuccess &&
-            b->out8.alloc(8, s) == cudaSuccess &&
-            b->cell7.alloc(7 * (size_t)ncells, s) == cudaSuccess;
+  cudaStream_t bs = b->bs;
+  const bool ok = b->x4.alloc(N, bs) == cudaSuccess && b->centers.alloc(N, bs) == cudaSuccess &&
+                  b->d_cell_off.alloc(ncells + 1, bs) == cudaSuccess &&
+                  b->f.alloc(3 * (size_t)N, bs) == cudaSuccess &&
+                  b->eatom.alloc(N, bs) == cudaSuccess &&
+                  b->vatom.alloc(6 * (size_t)N, bs) == cudaSuccess &&
+                  b->out8.alloc(8, bs) == cudaSuccess &&
+                  b->cell7.alloc(7 * (size_t)ncells, bs) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
-    delete b;
+    mlipg_batch_destroy(b);
     return MLIPG_ENOMEM;
   }
-  cudaMemcpyAsync(b->x4.p, hx4.data(), N * sizeof(double4), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(b->centers.p, hcent.data(), N * sizeof(int), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(b->off.p, hoff.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(b->idx.p, hidx.data(), hidx.size() * sizeof(int), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(b->img.p, himg.data(), himg.size() * sizeof(int), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(b->ccell.p, hcc.data(), N * sizeof(int), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(b->d_cell_off.p, aoff.data(), (ncells + 1) * sizeof(int),
-                  cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(b->lat.p, lattices, 9 * (size_t)ncells * sizeof(double),
-                  cudaMemcpyHostToDevice, s);
-  // Copies from pageable memory are staged before cudaMemcpyAsync returns,
-  // so the host vectors may go; the batch's work stays queued on the stream
-  // behind whatever the stream already holds.
-  if (cudaGetLastError() != cudaSuccess) {
-    delete b;
+  // copies from pageable memory are staged before cudaMemcpyAsync returns
+  if (cudaMemcpyAsync(b->x4.p, hx4.data(), N * sizeof(double4), cudaMemcpyHostToDevice, bs) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(b->d_cell_off.p, aoff.data(), (ncells + 1) * sizeof(int),
+                      cudaMemcpyHostToDevice, bs) != cudaSuccess) {
+    cudaGetLastError();
+    mlipg_batch_destroy(b);
     return MLIPG_ECUDA;
+  }
+  k_iota<<<(N + 255) / 256, 256, 0, bs>>>(N, b->centers.p);
+  int rc = mlipg_dnlist_create(bs, &b->nl);
+  if (rc == MLIPG_OK) rc = mlipg_dnlist_build(b->nl, ncells, natoms, lattices, b->x4.p,
+                                              mlipg_cutoff(h), 0);
+  if (rc == MLIPG_OK) {
+    int maxn = 0;
+    mlipg_dnlist_arrays(b->nl, nullptr, nullptr, nullptr, nullptr, nullptr, &b->npairs, &maxn,
+                        nullptr);
+    b->nb_cap = maxn;
+    if (cudaEventRecord(b->built, bs) != cudaSuccess) rc = MLIPG_ECUDA;
+  }
+  if (rc != MLIPG_OK) {
+    cudaGetLastError();
+    mlipg_batch_destroy(b);
+    return rc;
   }
   b->h_cell7.resize(7 * (size_t)ncells);
   *out = b;
@@ -198,11 +174,15 @@ extern "C" int mlipg_batch_create(mlipg_handle* h, int ncells, const int* natoms
 
 extern "C" int mlipg_batch_launch(mlipg_batch* b) {
   if (!b) return MLIPG_EINVAL;
-  if (cudaMemsetAsync(b->f.p, 0, 3 * (size_t)b->natoms * sizeof(double), b->s) != cudaSuccess)
+  const int *off = nullptr, *idx = nullptr, *img = nullptr, *ccell = nullptr;
+  const double* lat = nullptr;
+  mlipg_dnlist_arrays(b->nl, &off, &idx, &img, &ccell, &lat, nullptr, nullptr, nullptr);
+  if (cudaStreamWaitEvent(b->s, b->built, 0) != cudaSuccess ||
+      cudaMemsetAsync(b->f.p, 0, 3 * (size_t)b->natoms * sizeof(double), b->s) != cudaSuccess)
     return MLIPG_ECUDA;
-  int rc = mlipg_compute_device(b->h, b->natoms, b->x4.p, b->centers.p, b->off.p, b->idx.p,
-                                b->img.p, b->lat.p, b->ccell.p, nullptr, b->nb_cap, b->f.p,
-                                b->eatom.p, b->vatom.p, b->out8.p);
+  int rc = mlipg_compute_device(b->h, b->natoms, b->x4.p, b->centers.p, off, idx, img, lat,
+                                ccell, nullptr, b->nb_cap, b->f.p, b->eatom.p, b->vatom.p,
+                                b->out8.p);
   if (rc != MLIPG_OK) return rc;
   k_cell_sums<<<b->ncells, 128, 0, b->s>>>(b->d_cell_off.p, b->eatom.p, b->vatom.p, b->cell7.p);
   return cudaGetLastError() == cudaSuccess ? MLIPG_OK : MLIPG_ECUDA;
@@ -241,15 +221,19 @@ extern "C" int mlipg_batch_results(mlipg_batch* b, double* energies, double* for
 extern "C" int mlipg_batch_autotune(mlipg_batch* b, int max_report, double* report,
                                     int* nreport) {
   if (!b) return MLIPG_EINVAL;
-  return mlipg_autotune(b->h, b->natoms, b->x4.p, b->centers.p, b->off.p, b->idx.p, b->img.p,
-                        b->lat.p, b->ccell.p, b->nb_cap, b->f.p, b->out8.p, max_report, report,
-                        nreport);
+  const int *off = nullptr, *idx = nullptr, *img = nullptr, *ccell = nullptr;
+  const double* lat = nullptr;
+  mlipg_dnlist_arrays(b->nl, &off, &idx, &img, &ccell, &lat, nullptr, nullptr, nullptr);
+  if (cudaStreamWaitEvent(b->s, b->built, 0) != cudaSuccess) return MLIPG_ECUDA;
+  return mlipg_autotune(b->h, b->natoms, b->x4.p, b->centers.p, off, idx, img, lat, ccell,
+                        b->nb_cap, b->f.p, b->out8.p, max_report, report, nreport);
 }
 
 extern "C" size_t mlipg_batch_device_bytes(const mlipg_batch* b) {
   if (!b) return 0;
-  return (size_t)b->natoms * (sizeof(double4) + 4 + 4 + 4 + 24 + 8 + 48) +
-         (size_t)b->ncells * (9 * 8 + 4 + 56) + (size_t)b->npairs * 8;
+  // batch buffers + builder (cell, bin, count, offset per atom; bins; pairs)
+  return (size_t)b->natoms * (sizeof(double4) + 4 + 24 + 8 + 48 + 5 * 4) +
+         (size_t)b->ncells * (9 * 8 + 4 + 56 + 192) + (size_t)b->npairs * 8;
 }
 
 extern "C" int mlipg_batch_sizes(const mlipg_batch* b, int* natoms, long long* npairs) {
@@ -259,4 +243,9 @@ extern "C" int mlipg_batch_sizes(const mlipg_batch* b, int* natoms, long long* n
   return MLIPG_OK;
 }
 
-extern "C" void mlipg_batch_destroy(mlipg_batch* b) { delete b; }
+extern "C" void mlipg_batch_destroy(mlipg_batch* b) {
+  if (!b) return;
+  cudaStream_t bs = b->bs;
+  delete b;   // frees are queued on bs behind the last evaluation
+  if (bs) cudaStreamDestroy(bs);
+}

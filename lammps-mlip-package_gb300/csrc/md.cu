@@ -6,8 +6,8 @@
 // dtf = dt/2 * ftm2v, in LAMMPS metal units (A, ps, eV, g/mol).  Forces come
 // from the fused kernel through mlipg_compute_device with a full neighbour
 // list of owned atoms whose entries carry periodic image codes (no ghost
-// atoms), built with cutoff + skin and rebuilt when an atom has moved more
-// than skin/2 since the last build.  Each step is one CUDA graph launch
+// atoms), built on the device with cutoff + skin and rebuilt there when an
+// atom has moved more than skin/2 since the last build.  Each step is one CUDA graph launch
 // (integrate, zero forces, fused kernel, reduction, integrate, displacement
 // check) on the handle's stream.  Thermo (temperature, pressure tensor, total
 // energy) follows LAMMPS's `thermo_temp` / `pressure` computes: dof = 3N-3.
@@ -119,13 +119,14 @@ struct mlipg_md {
   std::vector<int> elem;
   std::vector<double> mass;
   DBuf<double4> x4;
-  DBuf<double> v, f, minv, m, xref, cell, out8, kin6;
-  DBuf<int> centers, off, idx, img, ccell, flag;
+  DBuf<double> v, f, minv, m, xref, out8, kin6;
+  DBuf<int> centers, flag;
+  mlipg_dnlist* nl = nullptr;   // device neighbour lists (image-coded, rc + skin)
+  int nl_gen = -1;
   cudaGraphExec_t graph = nullptr;
   double graph_dt = 0;
   int graph_tiling = 0;   // schedule generation the graph was captured with
   int* hflag = nullptr;
-  std::vector<double> hx;
 };
 
 #define MCK(call)                                                               \
@@ -136,57 +137,62 @@ struct mlipg_md {
     }                                                                           \
   } while (0)
 
-// (Re)builds the image-coded full list from host positions, uploads x4, xref.
-static int md_build_list(mlipg_md* md, const double* x) {
-  mlipg_nlist* nl = nullptr;
-  int rc = mlipg_nlist_build(md->lat, md->n, x, md->elem.data(), md->rc + md->skin, &nl);
-  if (rc != MLIPG_OK) return rc;
-  int nall = 0;
-  long long np = 0;
-  mlipg_nlist_sizes(nl, &nall, &np);
-  std::vector<double> xa((size_t)nall * 3);
-  std::vector<int> owner(nall), image(nall), off(md->n + 1), idx((size_t)std::max<long long>(np, 1));
-  mlipg_nlist_copy(nl, xa.data(), nullptr, owner.data(), image.data(), off.data(), idx.data());
-  mlipg_nlist_destroy(nl);
-  std::vector<int> img((size_t)std::max<long long>(np, 1));
-  int maxn = 0;
-  for (int i = 0; i < md->n; ++i) maxn = std::max(maxn, off[i + 1] - off[i]);
-  for (long long p = 0; p < np; ++p) {
-    const int j = idx[p];
-    img[p] = image[j];
-    idx[p] = owner[j];
-  }
-  std::vector<double4> x4(md->n);
-  for (int i = 0; i < md->n; ++i)
-    x4[i] = double4{xa[3 * i], xa[3 * i + 1], xa[3 * i + 2], (double)md->elem[i]};
-  MCK(md->x4.alloc(md->n));
-  MCK(md->xref.alloc((size_t)md->n * 3));
-  MCK(md->off.alloc(md->n + 1));
-  MCK(md->idx.alloc(idx.size()));
-  MCK(md->img.alloc(img.size()));
-  MCK(cudaMemcpyAsync(md->x4.p, x4.data(), md->n * sizeof(double4), cudaMemcpyHostToDevice, md->s));
-  MCK(cudaMemcpyAsync(md->xref.p, xa.data(), (size_t)md->n * 3 * sizeof(double),
-                      cudaMemcpyHostToDevice, md->s));
-  MCK(cudaMemcpyAsync(md->off.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice,
-                      md->s));
-  MCK(cudaMemcpyAsync(md->idx.p, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice,
-                      md->s));
-  MCK(cudaMemcpyAsync(md->img.p, img.data(), img.size() * sizeof(int), cudaMemcpyHostToDevice,
-                      md->s));
-  MCK(cudaStreamSynchronize(md->s));
-  md->nb_cap = maxn;
+__global__ void k_set_ref(int n, const double4* __restrict__ x4, double* __restrict__ xref) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4 p = x4[i];
+  xref[3 * i] = p.x;
+  xref[3 * i + 1] = p.y;
+  xref[3 * i + 2] = p.z;
+}
+
+static void md_drop_graph(mlipg_md* md) {
   if (md->graph) {
     cudaGraphExecDestroy(md->graph);
     md->graph = nullptr;
+  }
+}
+
+// (Re)builds the image-coded full list on the device from the positions in
+// x4 (uploaded from `x` first when given): wraps them into the cell and
+// records them as the displacement reference.  A captured step stays valid
+// unless a list array moved or the longest list outgrew the kernel's
+// neighbour capacity.
+static int md_build_list(mlipg_md* md, const double* x) {
+  if (x) {
+    std::vector<double4> x4(md->n);
+    for (int i = 0; i < md->n; ++i)
+      x4[i] = double4{x[3 * (size_t)i], x[3 * (size_t)i + 1], x[3 * (size_t)i + 2],
+                      (double)md->elem[i]};
+    MCK(md->x4.alloc(md->n));
+    MCK(md->xref.alloc((size_t)md->n * 3));
+    MCK(cudaMemcpyAsync(md->x4.p, x4.data(), md->n * sizeof(double4), cudaMemcpyHostToDevice,
+                        md->s));
+  }
+  const int rc = mlipg_dnlist_build(md->nl, 1, &md->n, md->lat, md->x4.p, md->rc + md->skin, 20);
+  if (rc != MLIPG_OK) return rc;
+  k_set_ref<<<(md->n + 255) / 256, 256, 0, md->s>>>(md->n, md->x4.p, md->xref.p);
+  MCK(cudaGetLastError());
+  int maxn = 0, gen = 0;
+  mlipg_dnlist_arrays(md->nl, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, &maxn, &gen);
+  if (maxn > md->nb_cap) {
+    md->nb_cap = maxn + maxn / 8;   // headroom: later rebuilds keep the captured step
+    md_drop_graph(md);
+  }
+  if (gen != md->nl_gen) {
+    md->nl_gen = gen;
+    md_drop_graph(md);
   }
   return MLIPG_OK;
 }
 
 static int md_forces(mlipg_md* md) {
   MCK(cudaMemsetAsync(md->f.p, 0, (size_t)md->n * 3 * sizeof(double), md->s));
-  return mlipg_compute_device(md->h, md->n, md->x4.p, md->centers.p, md->off.p, md->idx.p,
-                              md->img.p, md->cell.p, md->ccell.p, nullptr, md->nb_cap, md->f.p,
-                              nullptr, nullptr, md->out8.p);
+  const int *off = nullptr, *idx = nullptr, *img = nullptr, *ccell = nullptr;
+  const double* cell = nullptr;
+  mlipg_dnlist_arrays(md->nl, &off, &idx, &img, &ccell, &cell, nullptr, nullptr, nullptr);
+  return mlipg_compute_device(md->h, md->n, md->x4.p, md->centers.p, off, idx, img, cell, ccell,
+                              nullptr, md->nb_cap, md->f.p, nullptr, nullptr, md->out8.p);
 }
 
 // enqueues one velocity-Verlet step on the stream
@@ -234,15 +240,15 @@ extern "C" int mlipg_md_create(mlipg_handle* h, const double* lattice9, int nato
     md->mass[i] = mlipg_element_mass(h, elements[i]);
     minv[i] = 1.0 / md->mass[i];
   }
-  std::vector<int> cent(natoms), zero(natoms, 0);
+  std::vector<int> cent(natoms);
   for (int i = 0; i < natoms; ++i) cent[i] = i;
   std::vector<double> vv((size_t)natoms * 3, 0.0);
   if (v) std::memcpy(vv.data(), v, vv.size() * sizeof(double));
   if (md->v.alloc(vv.size()) != cudaSuccess || md->f.alloc(vv.size()) != cudaSuccess ||
       md->minv.alloc(natoms) != cudaSuccess || md->m.alloc(natoms) != cudaSuccess ||
-      md->cell.alloc(9) != cudaSuccess || md->out8.alloc(8) != cudaSuccess ||
-      md->kin6.alloc(6) != cudaSuccess || md->centers.alloc(natoms) != cudaSuccess ||
-      md->ccell.alloc(natoms) != cudaSuccess || md->flag.alloc(1) != cudaSuccess ||
+      md->out8.alloc(8) != cudaSuccess || md->kin6.alloc(6) != cudaSuccess ||
+      md->centers.alloc(natoms) != cudaSuccess || md->flag.alloc(1) != cudaSuccess ||
+      mlipg_dnlist_create(md->s, &md->nl) != MLIPG_OK ||
       cudaHostAlloc(&md->hflag, sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
     mlipg_md_destroy(md);
     return MLIPG_ENOMEM;
@@ -251,9 +257,7 @@ extern "C" int mlipg_md_create(mlipg_handle* h, const double* lattice9, int nato
   cudaMemcpyAsync(md->minv.p, minv.data(), natoms * sizeof(double), cudaMemcpyHostToDevice, md->s);
   cudaMemcpyAsync(md->m.p, md->mass.data(), natoms * sizeof(double), cudaMemcpyHostToDevice,
                   md->s);
-  cudaMemcpyAsync(md->cell.p, md->lat, 9 * sizeof(double), cudaMemcpyHostToDevice, md->s);
   cudaMemcpyAsync(md->centers.p, cent.data(), natoms * sizeof(int), cudaMemcpyHostToDevice, md->s);
-  cudaMemcpyAsync(md->ccell.p, zero.data(), natoms * sizeof(int), cudaMemcpyHostToDevice, md->s);
   cudaMemsetAsync(md->flag.p, 0, sizeof(int), md->s);
   int rc = md_build_list(md, x);
   if (rc == MLIPG_OK) rc = md_forces(md);
@@ -285,16 +289,8 @@ extern "C" int mlipg_md_run(mlipg_md* md, int nsteps, double dt, int use_graph) 
     MCK(cudaMemcpyAsync(md->hflag, md->flag.p, sizeof(int), cudaMemcpyDeviceToHost, md->s));
     MCK(cudaStreamSynchronize(md->s));
     if (*md->hflag) {
-      // an atom moved more than skin/2: rebuild from the current positions
-      std::vector<double4> x4(md->n);
-      MCK(cudaMemcpy(x4.data(), md->x4.p, md->n * sizeof(double4), cudaMemcpyDeviceToHost));
-      std::vector<double> x((size_t)md->n * 3);
-      for (int i = 0; i < md->n; ++i) {
-        x[3 * i] = x4[i].x;
-        x[3 * i + 1] = x4[i].y;
-        x[3 * i + 2] = x4[i].z;
-      }
-      rc = md_build_list(md, x.data());   // also drops the graph (pointers change)
+      // an atom moved more than skin/2: rebuild on the device
+      rc = md_build_list(md, nullptr);
       if (rc != MLIPG_OK) return rc;
       MCK(cudaMemsetAsync(md->flag.p, 0, sizeof(int), md->s));
       MCK(cudaStreamSynchronize(md->s));
@@ -367,5 +363,6 @@ extern "C" void mlipg_md_destroy(mlipg_md* md) {
   if (!md) return;
   if (md->graph) cudaGraphExecDestroy(md->graph);
   if (md->hflag) cudaFreeHost(md->hflag);
+  mlipg_dnlist_destroy(md->nl);
   delete md;
 }

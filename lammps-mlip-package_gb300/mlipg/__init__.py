@@ -93,6 +93,12 @@ def lib():
         "mlipg_get_tiling": (i32, [P, ip]),
         "mlipg_autotune": (i32, [P, i32, P, P, P, P, P, P, P, i32, P, P, i32, dp, ip]),
         "mlipg_batch_autotune": (i32, [P, i32, dp, ip]),
+        "mlipg_dnlist_create": (i32, [P, ctypes.POINTER(P)]),
+        "mlipg_dnlist_build": (i32, [P, i32, ip, dp, P, ctypes.c_double, i32]),
+        "mlipg_dnlist_arrays": (i32, [P, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P),
+                                      ctypes.POINTER(P), ctypes.POINTER(P), llp, ip, ip]),
+        "mlipg_dnlist_copy": (i32, [P, ip, ip, ip]),
+        "mlipg_dnlist_destroy": (None, [P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -470,6 +476,56 @@ class Server:
     def close(self):
         if getattr(self, "h", None):
             lib().mlipg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class DeviceNeighbourList:
+    """Image-coded full lists of many cells built on the device (mlipg_dnlist_*).
+
+    `build` takes a device pointer to double4 positions + element of all cells
+    (wrapped into their cells in place)."""
+
+    def __init__(self, stream: int = 0):
+        h = ctypes.c_void_p()
+        _check(lib().mlipg_dnlist_create(stream or None, ctypes.byref(h)))
+        self.h = h
+        self.natoms = 0
+
+    def build(self, natoms, lattices, x4_ptr: int, rlist: float, headroom_pct: int = 0):
+        n = np.ascontiguousarray(natoms, dtype=np.int32)
+        lat = np.ascontiguousarray(lattices, dtype=np.float64).reshape(-1, 9)
+        _check(lib().mlipg_dnlist_build(self.h, len(n), _ip(n), _dp(lat), x4_ptr, rlist,
+                                        headroom_pct))
+        self.natoms = int(n.sum())
+        return self.info()
+
+    def info(self):
+        ptrs = [ctypes.c_void_p() for _ in range(5)]
+        npairs = ctypes.c_longlong()
+        maxn = ctypes.c_int()
+        gen = ctypes.c_int()
+        _check(lib().mlipg_dnlist_arrays(self.h, *[ctypes.byref(p) for p in ptrs],
+                                         ctypes.byref(npairs), ctypes.byref(maxn),
+                                         ctypes.byref(gen)))
+        keys = ["off", "idx", "img", "center_cell", "cells"]
+        out = {k: p.value or 0 for k, p in zip(keys, ptrs)}
+        out.update(npairs=npairs.value, max_neigh=maxn.value, generation=gen.value)
+        return out
+
+    def copy(self):
+        info = self.info()
+        off = np.zeros(self.natoms + 1, dtype=np.int32)
+        idx = np.zeros(max(info["npairs"], 1), dtype=np.int32)
+        img = np.zeros(max(info["npairs"], 1), dtype=np.int32)
+        _check(lib().mlipg_dnlist_copy(self.h, _ip(off), _ip(idx), _ip(img)))
+        return off, idx[:info["npairs"]], img[:info["npairs"]]
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mlipg_dnlist_destroy(self.h)
             self.h = None
 
     def __del__(self):

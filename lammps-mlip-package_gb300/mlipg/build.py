@@ -53,6 +53,7 @@ def _sources():
         "noalloc.o": ("nvcc", os.path.join(CSRC, "noalloc.cu")),
         "md.o": ("nvcc", os.path.join(CSRC, "md.cu")),
         "batch.o": ("nvcc", os.path.join(CSRC, "batch.cu")),
+        "dnlist.o": ("nvcc", os.path.join(CSRC, "dnlist.cu")),
         "kernels_f64.o": ("nvcc", os.path.join(CSRC, "kernels_f64.cu")),
         "kernels_f32.o": ("nvcc", os.path.join(CSRC, "kernels_f32.cu")),
     }
