@@ -726,6 +726,7 @@ def run_md(args, dist):
     t0 = time.perf_counter()
     md = mlipg.MD(g, cell, v, skin=SKIN)
     setup_s = time.perf_counter() - t0
+    tune = {"table": md.autotune(), "picked": g.tiling()} if args.autotune else None
     md.run(args.warmup, spec["dt"], True)
     th0 = md.thermo()
     torch.cuda.synchronize()
@@ -760,7 +761,8 @@ def run_md(args, dist):
                                  "skin %.1f A, list rebuilt when an atom moves skin/2"
                                  % (spec["dt"], spec["temperature"], SKIN),
                            "step": "one CUDA graph per step (integrate, forces, integrate, "
-                                   "displacement check)"},
+                                   "displacement check)",
+                           "tiling": tune},
                 "thermo_start": th0, "thermo_end": th1,
                 "energy_drift_eV_per_atom": (th1["etotal"] - th0["etotal"]) / n,
                 "e2e": {"value": n * args.steps * dist["world"] / (el + setup_s), "unit": UNIT,

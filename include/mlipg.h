@@ -165,7 +165,9 @@ int mlipg_kernel_times(mlipg_handle* h, float* ms, int cap);
 /* With profiling on, SM cycles (summed over CTAs, thread-0 view) the fused
  * kernel spent in its phases since the last call: [0] neighbour compaction,
  * [1] order parameters, [2] nonlinear features + polynomial, [3] invariants
- * and adjoint, [4] forces and reductions. */
+ * and adjoint of the tuple-batched units (warp 0's share), [4] the remaining
+ * single-tuple units and the wait for the other warps, [5] forces and
+ * reductions. */
 int mlipg_phase_cycles(mlipg_handle* h, unsigned long long* out8);
 
 /* Live FMA throughput of the CUDA-core FP32 (fp64 = 0) or FP64 (fp64 = 1)
@@ -274,6 +276,9 @@ int mlipg_md_create(mlipg_handle* h, const double* lattice9, int natoms, const d
 int mlipg_md_run(mlipg_md* md, int nsteps, double dt_ps, int use_graph);
 int mlipg_md_state(mlipg_md* md, double* x, double* v, double* f);
 int mlipg_md_thermo(mlipg_md* md, double* out12);
+/* Autotunes the handle's tile shape on this system (see mlipg_autotune) and
+ * recomputes the forces at the current positions. */
+int mlipg_md_autotune(mlipg_md* md, int max_report, double* report, int* nreport);
 void mlipg_md_destroy(mlipg_md* md);
 
 /* Host neighbour-list builder for standalone and batched use: owned atoms

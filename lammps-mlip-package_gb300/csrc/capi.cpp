@@ -83,7 +83,7 @@ struct mlipg_handle {
   cudaStream_t stream = nullptr;
   // model tables on the device
   DevBuf d_terms, d_units, d_unit_off, d_nl, d_nl_off, d_poly, d_poly_off, d_wlin, d_radial;
-  DevBuf d_iunits, d_iunit_off, d_tuples, d_wlin_f, d_phase;
+  DevBuf d_iunits, d_iunit_off, d_tuples, d_wlin_f, d_phase, d_adj_base, d_adj_off, d_adj;
   // per-call buffers (grow only)
   DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_vatom, d_partials, d_status, d_out8;
   HostBuf h_x4, h_centers, h_off, h_idx, h_f, h_eatom, h_out;
@@ -131,6 +131,7 @@ static int upload_model(mlipg_handle* h) {
   std::vector<DeviceIrrUnit> iunits;
   std::vector<DeviceTuple> tuples;
   std::vector<int> uoff(M.T + 1, 0), noff(M.T + 1, 0), poff(M.T + 1, 0), ioff(M.T + 1, 0);
+  std::vector<int> abase(M.T + 1, 0), adj_off, adj;
   for (int t = 0; t < M.T; ++t) {
     const Schedule& S = M.sched[t];
     ioff[t] = (int)iunits.size();
@@ -146,6 +147,9 @@ static int upload_model(mlipg_handle* h) {
     units.insert(units.end(), S.units.begin(), S.units.end());
     nl.insert(nl.end(), S.nl_units.begin(), S.nl_units.end());
     poly.insert(poly.end(), S.poly.begin(), S.poly.end());
+    abase[t] = (int)adj_off.size();
+    for (int v : S.adj_off) adj_off.push_back((int)adj.size() + v);
+    for (int v : S.adj) adj.push_back((poff[t] + (v >> 2)) * 4 + (v & 3));
   }
   ioff[M.T] = (int)iunits.size();
   uoff[M.T] = (int)units.size();
@@ -167,6 +171,9 @@ static int upload_model(mlipg_handle* h) {
   CK(upload(h->d_nl_off, noff, s), "upload nonlinear offsets");
   CK(upload(h->d_poly, poly, s), "upload polynomial");
   CK(upload(h->d_poly_off, poff, s), "upload polynomial offsets");
+  CK(upload(h->d_adj_base, abase, s), "upload adjoint gather bases");
+  CK(upload(h->d_adj_off, adj_off, s), "upload adjoint gather offsets");
+  CK(upload(h->d_adj, adj, s), "upload adjoint gather lists");
   CK(upload(h->d_wlin, M.w_lin, s), "upload linear weights");
   {
     std::vector<float> wf(M.w_lin.begin(), M.w_lin.end());
@@ -240,7 +247,8 @@ int mlipg_destroy(mlipg_handle* h) {
     delete h;
     return MLIPG_OK;
   }
-  DevBuf* bufs[] = {&h->d_iunits, &h->d_iunit_off, &h->d_tuples, &h->d_wlin_f, &h->d_phase,
+  DevBuf* bufs[] = {&h->d_adj_base, &h->d_adj_off, &h->d_adj,
+                    &h->d_iunits, &h->d_iunit_off, &h->d_tuples, &h->d_wlin_f, &h->d_phase,
                     &h->d_terms, &h->d_units, &h->d_unit_off, &h->d_nl, &h->d_nl_off,
                     &h->d_poly, &h->d_poly_off, &h->d_wlin, &h->d_radial, &h->d_x4,
                     &h->d_centers, &h->d_off, &h->d_idx, &h->d_f, &h->d_eatom, &h->d_vatom, &h->d_partials,
@@ -353,6 +361,9 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.nl_off = h->d_nl_off.as<int>();
   a.poly = h->d_poly.as<DevicePoly>();
   a.poly_off = h->d_poly_off.as<int>();
+  a.adj_base = h->d_adj_base.as<int>();
+  a.adj_off = h->d_adj_off.as<int>();
+  a.adj = h->d_adj.as<int>();
   a.w_lin = h->d_wlin.as<double>();
   a.w_lin_f = h->d_wlin_f.as<float>();
   a.phase_clocks = h->profiling ? h->d_phase.as<unsigned long long>() : nullptr;
@@ -794,6 +805,9 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
   a.nl_off = h->d_nl_off.as<int>();
   a.poly = h->d_poly.as<DevicePoly>();
   a.poly_off = h->d_poly_off.as<int>();
+  a.adj_base = h->d_adj_base.as<int>();
+  a.adj_off = h->d_adj_off.as<int>();
+  a.adj = h->d_adj.as<int>();
   a.w_lin = h->d_wlin.as<double>();
   a.w_lin_f = h->d_wlin_f.as<float>();
   a.phase_clocks = h->profiling ? h->d_phase.as<unsigned long long>() : nullptr;

@@ -221,23 +221,36 @@ struct StageVis {
   }
 };
 
+// four consecutive values from 16-byte aligned shared memory
+__device__ __forceinline__ void load4(const float* p, float* v) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void load4(const double* p, double* v) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0];
+  const double2 b = reinterpret_cast<const double2*>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
 struct ForceVis {
-  const Rc* g;   // G of the neighbour's element slot, offset to channel n0: [Lh][16]
+  const R* g;    // Re G of the neighbour's element slot at channel n0: [Lh][16]; Im at g + gim
+  int gim;
   const R* f;    // f_n, f'_n of channels n0..n0+3
   const R* fd;
   R ux, uy, uz;
   R fx, fy, fz;
   __device__ __forceinline__ void operator()(int lmh, int mp, R yre, R yim, R xre, R xim, R yyre,
                                              R yyim, R zre, R zim) {
-    const Rc* gg = g + lmh * kNPad;
+    R gr[4], gi[4];
+    load4(g + lmh * kNPad, gr);
+    load4(g + gim + lmh * kNPad, gi);
     R g0r = 0, g0i = 0, g1r = 0, g1i = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const Rc v = gg[q];
-      g0r += f[q] * v.x;
-      g0i += f[q] * v.y;
-      g1r += fd[q] * v.x;
-      g1i += fd[q] * v.y;
+      g0r += f[q] * gr[q];
+      g0i += f[q] * gi[q];
+      g1r += fd[q] * gr[q];
+      g1i += fd[q] * gi[q];
     }
     const R coeff = (mp == 0) ? R(1) : R(2);
     const R ry = yre * g1r + yim * g1i;
@@ -276,8 +289,8 @@ __device__ __forceinline__ void pair_disp(const KernelArgs& A, int c, int k, con
 // One coupling unit for all n: warp halves take alternate terms.
 template <int Q, bool WITH_G>
 __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* __restrict__ terms,
-                                         const Rc* sa, Rc* sg, int Lh, int n, int half, bool act,
-                                         R H, R& dsum) {
+                                         const Rc* sa, R* sg, int gim, int Lh, int n, int half,
+                                         bool act, R H, R& dsum) {
   int off[Q];
 #pragma unroll
   for (int p = 0; p < Q; ++p) off[p] = (int)u.s[p] * Lh * kNPad + n;
@@ -335,9 +348,9 @@ __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* 
         const unsigned cd = (code >> (2 * p)) & 3u;
         const R kr = (cd == (unsigned)kSlotMZero) ? R(2) : R(1);
         if (act) {
-          Rc* gp = sg + off[p] + lmh[p] * kNPad;
-          atomicAdd(&gp->x, cc * kr * Pr);
-          if (cd < 2u) atomicAdd(&gp->y, (cd == 0u ? cc : -cc) * Pi);
+          R* gp = sg + off[p] + lmh[p] * kNPad;
+          atomicAdd(gp, cc * kr * Pr);
+          if (cd < 2u) atomicAdd(gp + gim, (cd == 0u ? cc : -cc) * Pi);
         }
       }
     }
@@ -356,18 +369,18 @@ __device__ __forceinline__ const R* wlin_table(const KernelArgs& A) {
 // element (u.s0) and covers the TT*TT tuples of the other two slots, which
 // keeps the unit's registers low enough for two resident CTAs per SM.  Per
 // term: order-parameter loads shared by all tuples, shared leave-one-out
-// products, per-tuple invariant sums d[j] (REAL) and adjoint partials per
-// (slot, element) in registers, flushed once per term.
+// products and adjoint partials per (slot, element) in registers, flushed
+// once per term; the unit's energy comes from the last slot's partials.
 template <int Q, int TT, bool FIX0>
 __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
                                         const R* __restrict__ wlin, const double* hnl,
-                                        const Rc* sa, Rc* sg, int Lh, int n, int half, bool act,
-                                        double& eacc) {
+                                        const Rc* sa, R* sg, int gim, int Lh, int n, int half,
+                                        bool act, double& eacc) {
   constexpr int N0 = FIX0 ? 1 : TT;                       // elements of slot 0 in this unit
   constexpr int NT = (Q == 1) ? N0 : (Q == 2 ? N0 * TT : N0 * TT * TT);
   const int s0base = FIX0 ? (int)u.s0 : 0;
-  R H[NT], d[NT];
+  R H[NT];
 #pragma unroll
   for (int j = 0; j < NT; ++j) {
     const int2 e = __ldg(reinterpret_cast<const int2*>(tups + u.tup + j));
@@ -377,8 +390,11 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       if (e.y >= 0) h = (R)((double)h + hnl[e.y * kNPad + n]);
     }
     H[j] = h;
-    d[j] = R(0);
   }
+  // Energy: sum_j H_j d_j of this unit's tuples, formed per term from the
+  // last slot's adjoint partial (sum_j H_j Pi_j = sum_s g_last[s] a_last[s]);
+  // the nonlinear part sum hnl d of H is subtracted once per centre.
+  R eu = R(0);
   const int es = Lh * kNPad;   // element stride in the a / G arrays
   const int kend = u.term0 + u.nterm;
   for (int k = u.term0 + half; k < kend; k += 2) {
@@ -418,22 +434,27 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
 #pragma unroll
       for (int s = 0; s < TT; ++s) { gr[p][s] = R(0); gi[p][s] = R(0); }
     if (Q == 1) {
+      R et = R(0);
 #pragma unroll
       for (int s0 = 0; s0 < N0; ++s0) {
-        d[s0] += ce * ar0[s0];
         g0r[s0] += H[s0];
+        et += H[s0] * ar0[s0];
       }
+      eu += ce * et;
     } else if (Q == 2) {
 #pragma unroll
       for (int s0 = 0; s0 < N0; ++s0)
 #pragma unroll
         for (int s1 = 0; s1 < TT; ++s1) {
           const int j = s0 * TT + s1;
-          d[j] += ce * (ar0[s0] * ar[1][s1] - ai0[s0] * ai[1][s1]);
           const R h = H[j];
           g0r[s0] += h * ar[1][s1]; g0i[s0] += h * ai[1][s1];
           gr[1][s1] += h * ar0[s0]; gi[1][s1] += h * ai0[s0];
         }
+      R et = R(0);
+#pragma unroll
+      for (int s1 = 0; s1 < TT; ++s1) et += gr[1][s1] * ar[1][s1] - gi[1][s1] * ai[1][s1];
+      eu += ce * et;
     } else {
       // b12[s1][s2] = a1 a2 (adjoint of slot 0)
       R b12r[TT][TT], b12i[TT][TT];
@@ -459,7 +480,6 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
 #pragma unroll
           for (int s2 = 0; s2 < TT; ++s2) {
             const int j = (s0 * TT + s1) * TT + s2;
-            d[j] += ce * (pr * ar[2][s2] - pi * ai[2][s2]);
             const R h = H[j];
             g0r[s0] += h * b12r[s1][s2]; g0i[s0] += h * b12i[s1][s2];
             gr[1][s1] += h * b02r[s2];   gi[1][s1] += h * b02i[s2];
@@ -467,6 +487,10 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
           }
         }
       }
+      R et = R(0);
+#pragma unroll
+      for (int s2 = 0; s2 < TT; ++s2) et += gr[2][s2] * ar[2][s2] - gi[2][s2] * ai[2][s2];
+      eu += ce * et;
     }
     if (act) {
 #pragma unroll
@@ -477,61 +501,53 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
         if (p == 0) {
 #pragma unroll
           for (int s = 0; s < N0; ++s) {
-            Rc* gp = sg + (s0base + s) * es + lo[0];
-            atomicAdd(&gp->x, kr * g0r[s]);
-            if (cd < 2u) atomicAdd(&gp->y, ki * g0i[s]);
+            R* gp = sg + (s0base + s) * es + lo[0];
+            atomicAdd(gp, kr * g0r[s]);
+            if (cd < 2u) atomicAdd(gp + gim, ki * g0i[s]);
           }
         } else {
 #pragma unroll
           for (int s = 0; s < TT; ++s) {
-            Rc* gp = sg + s * es + lo[p];
-            atomicAdd(&gp->x, kr * gr[p][s]);
-            if (cd < 2u) atomicAdd(&gp->y, ki * gi[p][s]);
+            R* gp = sg + s * es + lo[p];
+            atomicAdd(gp, kr * gr[p][s]);
+            if (cd < 2u) atomicAdd(gp + gim, ki * gi[p][s]);
           }
         }
       }
     }
   }
-  // combine the two half-warps' term sums; sum_j w_j d_j for this unit in
-  // REAL, accumulated into the centre's FP64 energy
-  R eu = R(0);
-#pragma unroll
-  for (int j = 0; j < NT; ++j) {
-    const R dj = d[j] + __shfl_xor_sync(0xffffffffu, d[j], 16);
-    const int itc = __ldg(reinterpret_cast<const int*>(tups + u.tup + j));
-    if (itc >= 0 && act) eu += __ldg(wlin + (size_t)itc * kNPad + n) * dj;
-  }
-  if (half == 0 && act) eacc += (double)eu;
+  // this half-warp's terms, in REAL, into the centre's FP64 energy
+  if (act) eacc += (double)eu;
 }
 
 template <int TT>
 __device__ __forceinline__ void dispatch_irr(const DeviceIrrUnit& u, const DeviceTuple* tups,
                                              const DeviceTerm* terms, const R* wlin,
-                                             const double* hnl, const Rc* sa, Rc* sg, int Lh,
-                                             int n, int half, bool act, double& eacc) {
+                                             const double* hnl, const Rc* sa, R* sg, int gim,
+                                             int Lh, int n, int half, bool act, double& eacc) {
   switch (u.q) {
-    case 1: run_irr<1, TT, false>(u, tups, terms, wlin, hnl, sa, sg, Lh, n, half, act, eacc); break;
-    case 2: run_irr<2, TT, false>(u, tups, terms, wlin, hnl, sa, sg, Lh, n, half, act, eacc); break;
+    case 1: run_irr<1, TT, false>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
+    case 2: run_irr<2, TT, false>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
     default:
       if (TT == 3)
-        run_irr<3, TT, true>(u, tups, terms, wlin, hnl, sa, sg, Lh, n, half, act, eacc);
+        run_irr<3, TT, true>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc);
       else
-        run_irr<3, TT, false>(u, tups, terms, wlin, hnl, sa, sg, Lh, n, half, act, eacc);
+        run_irr<3, TT, false>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc);
       break;
   }
 }
 
 template <bool WITH_G>
 __device__ __forceinline__ void dispatch_unit(const DeviceUnit& u, const DeviceTerm* terms,
-                                              const Rc* sa, Rc* sg, int Lh, int n, int half,
-                                              bool act, R H, R& dsum) {
+                                              const Rc* sa, R* sg, int gim, int Lh, int n,
+                                              int half, bool act, R H, R& dsum) {
   switch (u.q) {
-    case 1: run_unit<1, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
-    case 2: run_unit<2, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
-    case 3: run_unit<3, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
-    case 4: run_unit<4, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
-    case 5: run_unit<5, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
-    default: run_unit<6, WITH_G>(u, terms, sa, sg, Lh, n, half, act, H, dsum); break;
+    case 1: run_unit<1, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
+    case 2: run_unit<2, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
+    case 3: run_unit<3, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
+    case 4: run_unit<4, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
+    case 5: run_unit<5, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
+    default: run_unit<6, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
   }
 }
 
@@ -564,7 +580,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
   const int T = A.T, F = A.F, Lh = A.Lh, L = A.L;
   const SmemLayout lay = smem_layout(T, Lh, A.nb_cap, A.nl_cap);
   Rc* sa = reinterpret_cast<Rc*>(smem + lay.a);
-  Rc* sg = reinterpret_cast<Rc*>(smem + lay.g);
+  R* sg = reinterpret_cast<R*>(smem + lay.g);   // G: Re [T][Lh][16], then Im at sg + gim
+  const int gim = T * Lh * kNPad;
   double2* ys = reinterpret_cast<double2*>(sg);                     // P2 staging (FP64)
   double* fs = reinterpret_cast<double*>(smem + lay.g + (size_t)Lh * kChunk * sizeof(double2));
   double* dnl = reinterpret_cast<double*>(smem + lay.dnl);
@@ -726,12 +743,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     const int n = lane & 15, half = lane >> 4;
     const bool act = n < F;
     if (nNL > 0) {
-      for (int e = tid; e < nNL * kNPad; e += kBlock) hnl[e] = 0.0;
       __syncthreads();  // a[] complete
       for (int u = warp; u < nNL; u += kBlock / 32) {
         const DeviceUnit un = A.nl_units[nl0 + u];
         R dsum = R(0);
-        dispatch_unit<false>(un, A.terms, sa, sg, Lh, n, half, act, R(0), dsum);
+        dispatch_unit<false>(un, A.terms, sa, sg, gim, Lh, n, half, act, R(0), dsum);
         dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
         if (half == 0) dnl[u * kNPad + n] = act ? (double)dsum : 0.0;
       }
@@ -747,21 +763,31 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           prod *= v[q];
         }
         eacc += dp.w * prod;
+      }
+      // dE_poly/dd per nonlinear entry, gathered in a fixed order (no atomics,
+      // so the energies that weigh products with H stay reproducible)
+      const int ab = __ldg(A.adj_base + ti);
+      for (int e = tid; e < nNL * kNPad; e += kBlock) {
+        double h = 0.0;
+        const int x1 = __ldg(A.adj_off + ab + e + 1);
+        for (int x = __ldg(A.adj_off + ab + e); x < x1; ++x) {
+          const int v = __ldg(A.adj + x);
+          const DevicePoly dp = A.poly[v >> 2];
+          double o = dp.w;
 #pragma unroll
-        for (int q = 0; q < kMaxPoly; ++q) {
-          if (q < dp.order) {
-            double o = dp.w;
-#pragma unroll
-            for (int q2 = 0; q2 < kMaxPoly; ++q2)
-              if (q2 != q && q2 < dp.order) o *= v[q2];
-            atomicAdd(hnl + dp.k[q], o);
-          }
+          for (int q2 = 0; q2 < kMaxPoly; ++q2)
+            if (q2 != (v & 3) && q2 < dp.order) o *= dnl[dp.k[q2]];
+          h += o;
         }
+        hnl[e] = h;
       }
     }
     // ---------------------------------------------------------------- P4
-    for (int e = tid; e < T * Lh * kNPad; e += kBlock) sg[e] = Rc{R(0), R(0)};
+    for (int e = tid; e < 2 * gim; e += kBlock) sg[e] = R(0);
     __syncthreads();
+    // P5 weighs every feature's products with H = w + dE_poly/dd: remove the
+    // nonlinear part's share, sum hnl d over the nonlinear features
+    for (int e = tid; e < nNL * kNPad; e += kBlock) eacc -= hnl[e] * dnl[e];
     MLIPG_STAMP(2)
     // ---------------------------------------------------------------- P5
     {
@@ -774,12 +800,13 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         const DeviceIrrUnit iu = A.iunits[i0 + u];
         if (iu.nterm == 0) continue;   // padding of a balanced schedule
         if (T == 3)
-          dispatch_irr<3>(iu, A.tuples, A.terms, wl, hnl, sa, sg, Lh, n, half, act, eacc);
+          dispatch_irr<3>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, Lh, n, half, act, eacc);
         else if (T == 2)
-          dispatch_irr<2>(iu, A.tuples, A.terms, wl, hnl, sa, sg, Lh, n, half, act, eacc);
+          dispatch_irr<2>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, Lh, n, half, act, eacc);
         else
-          dispatch_irr<1>(iu, A.tuples, A.terms, wl, hnl, sa, sg, Lh, n, half, act, eacc);
+          dispatch_irr<1>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, Lh, n, half, act, eacc);
       }
+      MLIPG_STAMP(3)   // warp 0's batched units (the warps' shares are balanced)
       for (int u = warp; u < nU; u += kBlock / 32) {
         const DeviceUnit un = A.units[u0 + u];
         if (un.nterm == 0) continue;
@@ -789,13 +816,13 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           if (un.nl_slot >= 0) hv += hnl[un.nl_slot * kNPad + n];
         }
         R dsum = R(0);
-        dispatch_unit<true>(un, A.terms, sa, sg, Lh, n, half, act, (R)hv, dsum);
+        dispatch_unit<true>(un, A.terms, sa, sg, gim, Lh, n, half, act, (R)hv, dsum);
         dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
-        if (half == 0 && act) eacc += __ldg(A.w_lin + (size_t)un.itc * kNPad + n) * (double)dsum;
+        if (half == 0 && act) eacc += hv * (double)dsum;
       }
     }
     __syncthreads();
-    MLIPG_STAMP(3)
+    MLIPG_STAMP(4)
     // ---------------------------------------------------------------- P6
     double fix = 0.0, fiy = 0.0, fiz = 0.0;
     double va[6] = {0, 0, 0, 0, 0, 0};   // this centre's virial (reference order)
@@ -817,7 +844,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         R f[4], fd[4];
         radial4(A.radial, F, n0, (R)r, rc, f, fd);
         const double ir = 1.0 / r;
-        ForceVis v{sg + (size_t)tj * Lh * kNPad + n0, f, fd, (R)(dx * ir), (R)(dy * ir),
+        ForceVis v{sg + (size_t)tj * Lh * kNPad + n0, gim, f, fd, (R)(dx * ir), (R)(dy * ir),
                    (R)(dz * ir), R(0), R(0), R(0)};
         sh_visit<LCAP, true>((R)dx, (R)dy, (R)dz, (R)r, L, v);
         double fx = v.fx, fy = v.fy, fz = v.fz;
@@ -870,11 +897,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       atomicAdd(A.f + 3 * (size_t)fi + 2, gz);
     }
     __syncthreads();
-    MLIPG_STAMP(4)
+    MLIPG_STAMP(5)
   }
 #undef MLIPG_STAMP
   if (prof && tid == 0)
-    for (int k = 0; k < 5; ++k) atomicAdd(A.phase_clocks + k, ph[k]);
+    for (int k = 0; k < 6; ++k) atomicAdd(A.phase_clocks + k, ph[k]);
   // per-CTA partial sums: energy + virial (reference order)
   double vals[7] = {ecta, vir[0], vir[1], vir[2], vir[3], vir[4], vir[5]};
 #pragma unroll

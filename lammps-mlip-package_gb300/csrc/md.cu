@@ -334,6 +334,22 @@ extern "C" int mlipg_md_state(mlipg_md* md, double* x, double* v, double* f) {
   return MLIPG_OK;
 }
 
+// Autotunes the handle's tile shape on this system, then recomputes the
+// forces at the current positions (the tuning launches overwrite them).
+extern "C" int mlipg_md_autotune(mlipg_md* md, int max_report, double* report, int* nreport) {
+  if (!md) return MLIPG_EINVAL;
+  const int *off = nullptr, *idx = nullptr, *img = nullptr, *ccell = nullptr;
+  const double* cell = nullptr;
+  mlipg_dnlist_arrays(md->nl, &off, &idx, &img, &ccell, &cell, nullptr, nullptr, nullptr);
+  int rc = mlipg_autotune(md->h, md->n, md->x4.p, md->centers.p, off, idx, img, cell, ccell,
+                          md->nb_cap, md->f.p, md->out8.p, max_report, report, nreport);
+  if (rc != MLIPG_OK) return rc;
+  rc = md_forces(md);
+  if (rc != MLIPG_OK) return rc;
+  MCK(cudaStreamSynchronize(md->s));
+  return MLIPG_OK;
+}
+
 // out[0..10]: potential energy, kinetic energy, temperature (K), total energy,
 // pressure (bar), Pxx Pyy Pzz Pxy Pxz Pyz (bar), number of list rebuilds
 extern "C" int mlipg_md_thermo(mlipg_md* md, double* out12) {

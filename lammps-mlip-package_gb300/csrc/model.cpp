@@ -438,6 +438,19 @@ bool schedules_for_tiling(Model& M, std::string& err) {
         dp.k[p] = slot[row[p] % M.n_itc] * kNPad + row[p] / M.n_itc;
       S.poly.push_back(dp);
     }
+    {
+      const size_t ne = S.nl_units.size() * kNPad;
+      std::vector<std::vector<int>> lists(ne);
+      for (size_t pi = 0; pi < S.poly.size(); ++pi)
+        for (int q = 0; q < S.poly[pi].order; ++q)
+          lists[S.poly[pi].k[q]].push_back((int)pi * 4 + q);
+      S.adj_off.assign(ne + 1, 0);
+      S.adj.clear();
+      for (size_t e = 0; e < ne; ++e) {
+        S.adj.insert(S.adj.end(), lists[e].begin(), lists[e].end());
+        S.adj_off[e + 1] = (int)S.adj.size();
+      }
+    }
     (void)F;
     // every feature valid for this element is evaluated exactly once
     std::vector<int> seen(M.n_itc, 0);

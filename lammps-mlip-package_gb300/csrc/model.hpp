@@ -110,6 +110,10 @@ struct Schedule {         // per centre element
   std::vector<DeviceUnit> units;     // remaining valid itc, sorted by cost
   std::vector<DeviceUnit> nl_units;  // nonlinear itc, nl_slot = position
   std::vector<DevicePoly> poly;      // order >= 2 polynomial terms
+  // polynomial adjoint gather: entry e = slot*16 + n of the nonlinear
+  // features lists the (poly term, factor) pairs it receives, as p*4 + q
+  std::vector<int> adj_off;          // [nl_units.size()*16 + 1]
+  std::vector<int> adj;
 };
 
 struct Model {

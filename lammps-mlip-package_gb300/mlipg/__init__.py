@@ -93,6 +93,7 @@ def lib():
         "mlipg_get_tiling": (i32, [P, ip]),
         "mlipg_autotune": (i32, [P, i32, P, P, P, P, P, P, P, i32, P, P, i32, dp, ip]),
         "mlipg_batch_autotune": (i32, [P, i32, dp, ip]),
+        "mlipg_md_autotune": (i32, [P, i32, dp, ip]),
         "mlipg_dnlist_create": (i32, [P, ctypes.POINTER(P)]),
         "mlipg_dnlist_build": (i32, [P, i32, ip, dp, P, ctypes.c_double, i32]),
         "mlipg_dnlist_arrays": (i32, [P, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P),
@@ -303,13 +304,13 @@ class Potential:
                                                   nbr_idx, img, cell, center_cell, fold, nb_cap,
                                                   f, eatom, vatom, out8), self.h)
 
-    PHASES = ["compaction", "order_parameters", "nonlinear_polynomial", "invariants_adjoint",
-              "forces_reduction"]
+    PHASES = ["compaction", "order_parameters", "nonlinear_polynomial", "invariants_batched",
+              "invariants_single", "forces_reduction"]
 
     def phase_cycles(self):
         buf = (ctypes.c_ulonglong * 8)()
         _check(lib().mlipg_phase_cycles(self.h, buf), self.h)
-        return dict(zip(self.PHASES, [int(buf[k]) for k in range(5)]))
+        return dict(zip(self.PHASES, [int(buf[k]) for k in range(6)]))
 
     def device_status(self) -> int:
         b = ctypes.c_int()
@@ -342,6 +343,13 @@ class MD:
         rc = lib().mlipg_md_run(self.h, nsteps, dt, 1 if graph else 0)
         if rc != 0:
             raise MlipgError(rc, lib().mlipg_last_error(self.pot.h).decode())
+
+    def autotune(self):
+        """Picks the potential's tile shape for this system; returns the timing table."""
+        rep = np.zeros(4 * 64)
+        n = ctypes.c_int()
+        _check(lib().mlipg_md_autotune(self.h, 64, _dp(rep), ctypes.byref(n)), self.pot.h)
+        return _tiling_rows(rep, n.value)
 
     def state(self):
         x = np.zeros((self.n, 3))

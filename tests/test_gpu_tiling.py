@@ -94,3 +94,24 @@ def test_md_recaptures_graph_after_tiling_change(case):
     x, _, _ = md.state()
     md.close()
     assert np.abs(x - x_ref).max() <= 1e-9
+
+
+def test_md_autotune_keeps_trajectory(case):
+    pot, cells, _ = case
+    cell = cells[-1]
+    g = mlipg.Potential(pot, mlipg.PREC_FP64)
+    m = np.array(g.masses)[cell.types]
+    v0 = mlipg.maxwell_boltzmann(m, 300.0, np.random.default_rng(8))
+    ref = mlipg.MD(g, cell, v0)
+    ref.run(6, 0.001, True)
+    x_ref, v_ref, _ = ref.state()
+    ref.close()
+    md = mlipg.MD(g, cell, v0)
+    md.run(3, 0.001, True)
+    rows = md.autotune()
+    assert len(rows) >= 6
+    md.run(3, 0.001, True)
+    x, v, _ = md.state()
+    md.close()
+    assert np.abs(x - x_ref).max() <= 1e-9
+    assert np.abs(v - v_ref).max() <= 1e-8

@@ -29,8 +29,12 @@ def _device_inputs(s, dev):
         i=torch.from_numpy(s.nbr_idx).to(dev))
 
 
-@pytest.mark.parametrize("prec,tol", [(mlipg.PREC_FP64, 1e-10), (mlipg.PREC_MIXED, 5e-5)])
+@pytest.mark.parametrize("prec,tol", [(mlipg.PREC_FP64, 1e-12), (mlipg.PREC_MIXED, 5e-6)])
 def test_noalloc_matches_regular_entry_point(potdir, prec, tol):
+    """Both entry points run the same kernel; they differ only through the order
+    of the atomic additions, so the no-allocation results agree with the
+    regular ones as closely as two regular calls agree with each other (four
+    times their spread), or within `tol` of each array's scale."""
     import torch
     dev = torch.device("cuda")
     g = mlipg.Potential(potdir["gtinv-820"], prec)
@@ -50,9 +54,11 @@ def test_noalloc_matches_regular_entry_point(potdir, prec, tol):
         return f.cpu().numpy(), out.cpu().numpy(), ea.cpu().numpy(), va.cpu().numpy()
 
     ref = run(g.compute_device)
+    ref2 = run(g.compute_device)
+    spread = [np.abs(a - b).max() for a, b in zip(ref, ref2)]
     for _ in range(2):                      # two calls in a row share the scratch
         got = run(g.compute_device_noalloc)
-        for a, b in zip(got, ref):
+        for a, b, sp in zip(got, ref, spread):
             scale = max(np.abs(b).max(), 1e-300)
-            assert np.abs(a - b).max() <= tol * scale
+            assert np.abs(a - b).max() <= max(4.0 * sp, tol * scale)
         assert got[1][0] == pytest.approx(got[2].sum(), rel=1e-12)
