@@ -364,22 +364,22 @@ __device__ __forceinline__ const R* wlin_table(const KernelArgs& A) {
   return wlin_pick(A.w_lin, A.w_lin_f, (R*)nullptr);
 }
 
-// Element tuples of one irreps (order Q <= 3, TT elements) over a chunk of
-// canonical terms.  For Q = 3 and TT = 3 a unit fixes the first slot's
-// element (u.s0) and covers the TT*TT tuples of the other two slots, which
-// keeps the unit's registers low enough for two resident CTAs per SM.  Per
-// term: order-parameter loads shared by all tuples, shared leave-one-out
-// products and adjoint partials per (slot, element) in registers, flushed
-// once per term; the unit's energy comes from the last slot's partials.
-template <int Q, int TT, bool FIX0>
-__device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
+// Direct form for up to two elements and orders <= 3: every tuple of the
+// unit (TT^Q of them, all elements of every slot) is formed from shared
+// leave-one-out products, with adjoint partials per (slot, element) in
+// registers flushed once per term; the unit's energy comes from the last
+// slot's partials (sum_j H_j Pi_j = sum_s g_last[s] a_last[s]).  Shorter
+// dependency chains than the factorized form, which pays off only with
+// three elements.
+template <int Q, int TT>
+__device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
                                         const R* __restrict__ wlin, const double* hnl,
                                         const Rc* sa, R* sg, int gim, int Lh, int n, int half,
                                         bool act, double& eacc) {
-  constexpr int N0 = FIX0 ? 1 : TT;                       // elements of slot 0 in this unit
+  constexpr int N0 = TT;                                  // elements of slot 0
   constexpr int NT = (Q == 1) ? N0 : (Q == 2 ? N0 * TT : N0 * TT * TT);
-  const int s0base = FIX0 ? (int)u.s0 : 0;
+  constexpr int s0base = 0;
   R H[NT];
 #pragma unroll
   for (int j = 0; j < NT; ++j) {
@@ -520,20 +520,206 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
   if (act) eacc += (double)eu;
 }
 
+// Element tuples of one irreps (order Q <= 4, TT elements) over a chunk of
+// canonical terms.  Order 4 fixes the element of slot 0 per unit (u.s0; its
+// order parameter is the prefix A); the last three slots z, x, y (the last
+// two, x and y, for Q = 2; slot 0 alone for Q = 1) run over all elements.
+// With H[z][x][y] the features' adjoint weights and a, b, c the order
+// parameters of slots z, x, y, per term and per element z:
+//   m[x] = sum_y H c[y],  w[y] = sum_x H b[x],  S_z = sum_x b[x] m[x],
+//   G_z[z] += A S_z,  G_x[x] += A a[z] m[x],  G_y[y] += A a[z] w[y],
+// and with S = sum_z a[z] S_z:  G_0 += S (order 4), energy += Re(A S)
+// (= the sum over tuples of H times the tuple's invariant term).  One set of
+// order-parameter loads per term; the adjoint partials of x and y are summed
+// over z in registers and flushed with one shared-memory atomic per (slot,
+// element).
+template <int Q, int TT>
+__device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
+                                        const DeviceTerm* __restrict__ terms,
+                                        const R* __restrict__ wlin, const double* hnl,
+                                        const Rc* sa, R* sg, int gim, int Lh, int n, int half,
+                                        bool act, double& eacc) {
+  constexpr int NZ = (Q >= 3) ? TT : 1;      // elements of slot z
+  constexpr int NX = TT;                     // elements of slot x (slot 0 for Q = 1)
+  constexpr int NY = (Q == 1) ? 1 : TT;      // elements of slot y
+  constexpr int PZ = Q - 3;                  // slot indices (PZ, PY unused when absent)
+  constexpr int PX = (Q == 1) ? 0 : Q - 2;
+  constexpr int PY = Q - 1;
+  R H[NZ][NX][NY];
+#pragma unroll
+  for (int z = 0; z < NZ; ++z)
+#pragma unroll
+    for (int x = 0; x < NX; ++x)
+#pragma unroll
+      for (int y = 0; y < NY; ++y) {
+        const int2 e =
+            __ldg(reinterpret_cast<const int2*>(tups + u.tup + (z * NX + x) * NY + y));
+        R h = R(0);
+        if (act && e.x >= 0) {
+          h = __ldg(wlin + (size_t)e.x * kNPad + n);
+          if (e.y >= 0) h = (R)((double)h + hnl[e.y * kNPad + n]);
+        }
+        H[z][x][y] = h;
+      }
+  const int s0 = (int)u.s0;
+  const int es = Lh * kNPad;   // element stride in the a / G arrays
+  R eu = R(0);
+  const int kend = u.term0 + u.nterm;
+  for (int k = u.term0 + half; k < kend; k += 2) {
+    const int4 raw = __ldg(reinterpret_cast<const int4*>(terms + k));
+    const R c = (R)__hiloint2double(raw.y, raw.x);
+    const unsigned lw = (unsigned)raw.z, code = ((unsigned)raw.w) >> 16;
+    const bool self = (code >> 12) & 1u;
+    const R ce = self ? c : R(2) * c;
+    int lo[Q];
+#pragma unroll
+    for (int p = 0; p < Q; ++p) lo[p] = (int)((lw >> (8 * p)) & 255u) * kNPad + n;
+    const auto conj_of = [&](int p) { return ((code >> (2 * p)) & 3u) == (unsigned)kSlotConj; };
+    R Ar = R(1), Ai = R(0);   // fixed slot 0 of order 4
+    if (Q == 4) {
+      const Rc v = sa[s0 * es + lo[0]];
+      Ar = v.x;
+      Ai = conj_of(0) ? -v.y : v.y;
+    }
+    R zr[NZ], zi[NZ], br[NX], bi[NX], cr[NY], ci[NY];
+    if (Q >= 3) {
+      const bool cj = conj_of(PZ);
+#pragma unroll
+      for (int z = 0; z < NZ; ++z) {
+        const Rc v = sa[z * es + lo[PZ]];
+        zr[z] = v.x;
+        zi[z] = cj ? -v.y : v.y;
+      }
+    } else {
+      zr[0] = R(1);
+      zi[0] = R(0);
+    }
+    {
+      const bool cj = conj_of(PX);
+#pragma unroll
+      for (int x = 0; x < NX; ++x) {
+        const Rc v = sa[x * es + lo[PX]];
+        br[x] = v.x;
+        bi[x] = cj ? -v.y : v.y;
+      }
+    }
+    if (Q > 1) {
+      const bool cj = conj_of(PY);
+#pragma unroll
+      for (int y = 0; y < NY; ++y) {
+        const Rc v = sa[y * es + lo[PY]];
+        cr[y] = v.x;
+        ci[y] = cj ? -v.y : v.y;
+      }
+    }
+    // adjoint partials summed over z: x and y (before the prefix A), and S
+    R gxr[NX], gxi[NX], gyr[NY], gyi[NY], gzr[NZ], gzi[NZ];
+    R Sr = R(0), Si = R(0);
+#pragma unroll
+    for (int x = 0; x < NX; ++x) { gxr[x] = R(0); gxi[x] = R(0); }
+#pragma unroll
+    for (int y = 0; y < NY; ++y) { gyr[y] = R(0); gyi[y] = R(0); }
+#pragma unroll
+    for (int z = 0; z < NZ; ++z) {
+      R mr[NX], mi[NX];
+#pragma unroll
+      for (int x = 0; x < NX; ++x) {
+        if (Q == 1) {
+          mr[x] = H[0][x][0];
+          mi[x] = R(0);
+        } else {
+          R tr = R(0), ti = R(0);
+#pragma unroll
+          for (int y = 0; y < NY; ++y) {
+            tr += H[z][x][y] * cr[y];
+            ti += H[z][x][y] * ci[y];
+          }
+          mr[x] = tr;
+          mi[x] = ti;
+        }
+      }
+      R szr = R(0), szi = R(0);
+#pragma unroll
+      for (int x = 0; x < NX; ++x) {
+        szr += br[x] * mr[x] - bi[x] * mi[x];
+        szi += br[x] * mi[x] + bi[x] * mr[x];
+      }
+      gzr[z] = szr;
+      gzi[z] = szi;
+      Sr += zr[z] * szr - zi[z] * szi;
+      Si += zr[z] * szi + zi[z] * szr;
+#pragma unroll
+      for (int x = 0; x < NX; ++x) {
+        gxr[x] += zr[z] * mr[x] - zi[z] * mi[x];
+        gxi[x] += zr[z] * mi[x] + zi[z] * mr[x];
+      }
+      if (Q > 1) {
+#pragma unroll
+        for (int y = 0; y < NY; ++y) {
+          R tr = R(0), ti = R(0);
+#pragma unroll
+          for (int x = 0; x < NX; ++x) {
+            tr += H[z][x][y] * br[x];
+            ti += H[z][x][y] * bi[x];
+          }
+          gyr[y] += zr[z] * tr - zi[z] * ti;
+          gyi[y] += zr[z] * ti + zi[z] * tr;
+        }
+      }
+    }
+    eu += ce * (Ar * Sr - Ai * Si);
+    if (act) {
+      // adjoint of slot p: A * partial, scaled by (kr, ki) from its storage code
+      const auto flush = [&](int p, int e, R vr, R vi) {
+        const unsigned cd = (code >> (2 * p)) & 3u;
+        const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
+        const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
+        R* gp = sg + e * es + lo[p];
+        atomicAdd(gp, kr * (Ar * vr - Ai * vi));
+        if (cd < 2u) atomicAdd(gp + gim, ki * (Ar * vi + Ai * vr));
+      };
+#pragma unroll
+      for (int x = 0; x < NX; ++x) flush(PX, x, gxr[x], gxi[x]);
+      if (Q > 1) {
+#pragma unroll
+        for (int y = 0; y < NY; ++y) flush(PY, y, gyr[y], gyi[y]);
+      }
+      if (Q >= 3) {
+#pragma unroll
+        for (int z = 0; z < NZ; ++z) flush(PZ, z, gzr[z], gzi[z]);
+      }
+      if (Q == 4) {   // slot 0: S, without the prefix A (it is slot 0's own factor)
+        const unsigned cd = code & 3u;
+        const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
+        const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
+        R* gp = sg + s0 * es + lo[0];
+        atomicAdd(gp, kr * Sr);
+        if (cd < 2u) atomicAdd(gp + gim, ki * Si);
+      }
+    }
+  }
+  // this half-warp's terms, in REAL, into the centre's FP64 energy
+  if (act) eacc += (double)eu;
+}
+
 template <int TT>
 __device__ __forceinline__ void dispatch_irr(const DeviceIrrUnit& u, const DeviceTuple* tups,
                                              const DeviceTerm* terms, const R* wlin,
                                              const double* hnl, const Rc* sa, R* sg, int gim,
                                              int Lh, int n, int half, bool act, double& eacc) {
+  if (TT <= 2 && u.q <= 3) {
+    switch (u.q) {
+      case 1: run_irr_direct<1, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
+      case 2: run_irr_direct<2, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
+      default: run_irr_direct<3, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
+    }
+    return;
+  }
   switch (u.q) {
-    case 1: run_irr<1, TT, false>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
-    case 2: run_irr<2, TT, false>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
-    default:
-      if (TT == 3)
-        run_irr<3, TT, true>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc);
-      else
-        run_irr<3, TT, false>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc);
-      break;
+    case 1: run_irr<1, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
+    case 2: run_irr<2, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
+    case 3: run_irr<3, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
+    default: run_irr<4, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
   }
 }
 

@@ -356,7 +356,7 @@ bool schedules_for_tiling(Model& M, std::string& err) {
       slot[i] = u.nl_slot;
       S.nl_units.push_back(u);
     }
-    // batched-tuple units for orders <= 3 when T <= 3
+    // batched-tuple units for orders <= 4 when T <= 3
     std::vector<char> covered(M.n_itc, 0);
     if (T <= 3) {
       std::map<std::pair<int, std::vector<int>>, int> itc_of;
@@ -364,7 +364,7 @@ bool schedules_for_tiling(Model& M, std::string& err) {
       for (int k = 0; k < (int)M.irr_l.size(); ++k) {
         const auto& lc = M.irr_l[k];
         const int q = (int)lc.size();
-        if (q > 3) continue;
+        if (q > 4) continue;
         int nt = 1;
         for (int p = 0; p < q; ++p) nt *= T;
         const int tup0 = (int)S.tuples.size();
@@ -387,19 +387,25 @@ bool schedules_for_tiling(Model& M, std::string& err) {
           }
           S.tuples.push_back(d);
         }
-        // order 3 with 3 elements: one unit per element of slot 0 (T*T tuples each)
-        const bool fix0 = (q == 3 && T == 3);
-        const int nsub = fix0 ? T : 1;
-        for (int s0 = 0; s0 < nsub; ++s0)
+        // order 4: one unit per element of slot 0, each over the T^3 tuples
+        // of the other slots; lower orders: one unit over all T^q tuples;
+        // blocks without any feature are skipped
+        const int nsub = q == 4 ? T : 1;
+        const int block = q == 1 ? T : (q == 2 ? T * T : T * T * T);
+        for (int f = 0; f < nsub; ++f) {
+          bool any = false;
+          for (int j = 0; j < block; ++j) any = any || S.tuples[tup0 + f * block + j].itc >= 0;
+          if (!any) continue;
           for (int c0 = 0; c0 < M.irr_cnterms[k]; c0 += M.tiling.irr_chunk) {
             DeviceIrrUnit iu{};
             iu.term0 = M.irr_cfirst[k] + c0;
             iu.nterm = std::min(M.tiling.irr_chunk, M.irr_cnterms[k] - c0);
-            iu.tup = tup0 + (fix0 ? s0 * T * T : 0);
+            iu.tup = tup0 + f * block;
             iu.q = (uint8_t)q;
-            iu.s0 = (uint8_t)s0;
+            iu.s0 = (uint8_t)f;
             S.iunits.push_back(iu);
           }
+        }
       }
       std::stable_sort(S.iunits.begin(), S.iunits.end(),
                        [](const DeviceIrrUnit& a, const DeviceIrrUnit& b) {
@@ -464,11 +470,11 @@ bool schedules_for_tiling(Model& M, std::string& err) {
       }
     if (M.tiling.warp_order == 1) {
       // per-warp cost ~ terms x tuples x order (products and adjoint products)
+      // batched unit per term: products over the tuple block, one atomic
+      // pair per (slot, element)
       const auto icost = [&](const DeviceIrrUnit& u) {
-        int nt = 1;
-        for (int p = 0; p < u.q; ++p) nt *= T;
-        if (u.q == 3 && T == 3) nt /= T;
-        return (double)u.nterm * nt * u.q;
+        const double nz = u.q >= 3 ? T : 1;
+        return (double)u.nterm * (u.q == 1 ? 2.0 * T : nz * 8.0 * T * T + 12.0 * T * (u.q - 1));
       };
       const auto ucost = [](const DeviceUnit& u) { return (double)u.nterm * u.q; };
       double load[kCtaWarps] = {};

@@ -67,17 +67,19 @@ struct DevicePoly {       // 32 bytes
   int pad;
 };
 
-// All element tuples of one irreps (orders 1..3, up to 3 elements) over a
-// chunk of its canonical terms: the kernel evaluates every tuple of the
-// chunk per term from one set of order-parameter loads.  Tuples are ordered
-// lexicographically over T^q; the DeviceTuple array at `tup` maps each to its
-// itc (or -1 for orderings that are not the canonical multiset order).
+// Element tuples of one irreps (orders 1..4, up to 3 elements) over a chunk
+// of its canonical terms.  Order-4 units fix the element of slot 0 (s0) and
+// cover the T^3 tuples of the other slots; lower orders cover all T^q tuples;
+// one set of order-parameter loads per term.  Tuples are ordered
+// lexicographically over T^q; the DeviceTuple block at `tup` maps each of
+// the unit's tuples to its itc (or -1 for orderings that are not the
+// canonical multiset order).
 struct DeviceIrrUnit {    // 16 bytes
   int term0;
   int nterm;
-  int tup;                // first DeviceTuple of this unit (T^(q-1) of them when s0 is fixed)
+  int tup;                // first DeviceTuple of this unit's block
   uint8_t q;
-  uint8_t s0;             // element of slot 0 for order-3 units with 3 elements
+  uint8_t s0;             // fixed element of slot 0 (order 4)
   uint8_t pad[2];
 };
 struct DeviceTuple {      // 8 bytes
