@@ -328,7 +328,7 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   const bool fp64 = h->precision == MLIPG_PREC_FP64;
   nb_cap = std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
   const int nl_cap = std::max(M.max_nl, 1);
-  const size_t smem = fused_smem_bytes(fp64, M.T, M.Lh, nb_cap, nl_cap);
+  const size_t smem = fused_smem_bytes(fp64, M.T, M.L, nb_cap, nl_cap);
   if (smem > 227 * 1024)
     return fail(h, MLIPG_ENOTSUP,
                 "model needs %zu bytes of shared memory per CTA (limit 232448): "
@@ -698,7 +698,7 @@ extern "C" int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4,
   const Model& M = h->model;
   const bool fp64 = h->precision == MLIPG_PREC_FP64;
   const int cap = std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
-  const size_t smem = fused_smem_bytes(fp64, M.T, M.Lh, cap, std::max(M.max_nl, 1));
+  const size_t smem = fused_smem_bytes(fp64, M.T, M.L, cap, std::max(M.max_nl, 1));
   const int bps_max = std::max(1, fused_max_blocks_per_sm(fp64, M.L, smem));
   // a sample of 16 centres per resident CTA keeps each candidate short
   const int sample = std::min(ncenters, 16 * bps_max * h->num_sms);
@@ -773,7 +773,7 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
   const bool fp64 = h->precision == MLIPG_PREC_FP64;
   nb_cap = std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
   const int nl_cap = std::max(M.max_nl, 1);
-  const size_t smem = fused_smem_bytes(fp64, M.T, M.Lh, nb_cap, nl_cap);
+  const size_t smem = fused_smem_bytes(fp64, M.T, M.L, nb_cap, nl_cap);
   if (smem > 227 * 1024)
     return fail(h, MLIPG_ENOTSUP, "model needs %zu bytes of shared memory per CTA", smem);
   int bps = fused_max_blocks_per_sm(fp64, M.L, smem);

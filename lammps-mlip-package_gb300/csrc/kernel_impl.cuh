@@ -287,9 +287,9 @@ __device__ __forceinline__ void pair_disp(const KernelArgs& A, int c, int k, con
 }
 
 // One coupling unit for all n: warp halves take alternate terms.
-template <int Q, bool WITH_G>
+template <int Q, bool WITH_G, int Lh>
 __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* __restrict__ terms,
-                                         const Rc* sa, R* sg, int gim, int Lh, int n, int half,
+                                         const Rc* sa, R* sg, int gim, int n, int half,
                                          bool act, R H, R& dsum) {
   int off[Q];
 #pragma unroll
@@ -371,11 +371,11 @@ __device__ __forceinline__ const R* wlin_table(const KernelArgs& A) {
 // slot's partials (sum_j H_j Pi_j = sum_s g_last[s] a_last[s]).  Shorter
 // dependency chains than the factorized form, which pays off only with
 // three elements.
-template <int Q, int TT>
+template <int Q, int TT, int Lh>
 __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
                                         const R* __restrict__ wlin, const double* hnl,
-                                        const Rc* sa, R* sg, int gim, int Lh, int n, int half,
+                                        const Rc* sa, R* sg, int gim, int n, int half,
                                         bool act, double& eacc) {
   constexpr int N0 = TT;                                  // elements of slot 0
   constexpr int NT = (Q == 1) ? N0 : (Q == 2 ? N0 * TT : N0 * TT * TT);
@@ -395,7 +395,7 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
   // last slot's adjoint partial (sum_j H_j Pi_j = sum_s g_last[s] a_last[s]);
   // the nonlinear part sum hnl d of H is subtracted once per centre.
   R eu = R(0);
-  const int es = Lh * kNPad;   // element stride in the a / G arrays
+  constexpr int es = Lh * kNPad;   // element stride in the a / G arrays
   const int kend = u.term0 + u.nterm;
   for (int k = u.term0 + half; k < kend; k += 2) {
     const int4 raw = __ldg(reinterpret_cast<const int4*>(terms + k));
@@ -533,11 +533,11 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
 // order-parameter loads per term; the adjoint partials of x and y are summed
 // over z in registers and flushed with one shared-memory atomic per (slot,
 // element).
-template <int Q, int TT>
+template <int Q, int TT, int Lh>
 __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
                                         const R* __restrict__ wlin, const double* hnl,
-                                        const Rc* sa, R* sg, int gim, int Lh, int n, int half,
+                                        const Rc* sa, R* sg, int gim, int n, int half,
                                         bool act, double& eacc) {
   constexpr int NZ = (Q >= 3) ? TT : 1;      // elements of slot z
   constexpr int NX = TT;                     // elements of slot x (slot 0 for Q = 1)
@@ -562,7 +562,7 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
         H[z][x][y] = h;
       }
   const int s0 = (int)u.s0;
-  const int es = Lh * kNPad;   // element stride in the a / G arrays
+  constexpr int es = Lh * kNPad;   // element stride in the a / G arrays
   R eu = R(0);
   const int kend = u.term0 + u.nterm;
   for (int k = u.term0 + half; k < kend; k += 2) {
@@ -702,38 +702,38 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
   if (act) eacc += (double)eu;
 }
 
-template <int TT>
+template <int TT, int Lh>
 __device__ __forceinline__ void dispatch_irr(const DeviceIrrUnit& u, const DeviceTuple* tups,
                                              const DeviceTerm* terms, const R* wlin,
                                              const double* hnl, const Rc* sa, R* sg, int gim,
-                                             int Lh, int n, int half, bool act, double& eacc) {
+                                             int n, int half, bool act, double& eacc) {
   if (TT <= 2 && u.q <= 3) {
     switch (u.q) {
-      case 1: run_irr_direct<1, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
-      case 2: run_irr_direct<2, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
-      default: run_irr_direct<3, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
+      case 1: run_irr_direct<1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
+      case 2: run_irr_direct<2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
+      default: run_irr_direct<3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
     }
     return;
   }
   switch (u.q) {
-    case 1: run_irr<1, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
-    case 2: run_irr<2, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
-    case 3: run_irr<3, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
-    default: run_irr<4, TT>(u, tups, terms, wlin, hnl, sa, sg, gim, Lh, n, half, act, eacc); break;
+    case 1: run_irr<1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
+    case 2: run_irr<2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
+    case 3: run_irr<3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
+    default: run_irr<4, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
   }
 }
 
-template <bool WITH_G>
+template <bool WITH_G, int Lh>
 __device__ __forceinline__ void dispatch_unit(const DeviceUnit& u, const DeviceTerm* terms,
-                                              const Rc* sa, R* sg, int gim, int Lh, int n,
+                                              const Rc* sa, R* sg, int gim, int n,
                                               int half, bool act, R H, R& dsum) {
   switch (u.q) {
-    case 1: run_unit<1, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
-    case 2: run_unit<2, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
-    case 3: run_unit<3, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
-    case 4: run_unit<4, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
-    case 5: run_unit<5, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
-    default: run_unit<6, WITH_G>(u, terms, sa, sg, gim, Lh, n, half, act, H, dsum); break;
+    case 1: run_unit<1, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
+    case 2: run_unit<2, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
+    case 3: run_unit<3, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
+    case 4: run_unit<4, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
+    case 5: run_unit<5, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
+    default: run_unit<6, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
   }
 }
 
@@ -764,10 +764,13 @@ template <int LCAP>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_constant__ KernelArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int T = A.T, F = A.F, Lh = A.Lh, L = A.L;
-  const SmemLayout lay = smem_layout(T, Lh, A.nb_cap, A.nl_cap);
+  // rows of the a / G arrays per element: the instantiation's capacity, so
+  // that element strides are compile-time constants (rows >= Lh are unused)
+  constexpr int LS = (LCAP + 1) * (LCAP + 2) / 2;
+  const SmemLayout lay = smem_layout(T, LS, A.nb_cap, A.nl_cap);
   Rc* sa = reinterpret_cast<Rc*>(smem + lay.a);
   R* sg = reinterpret_cast<R*>(smem + lay.g);   // G: Re [T][Lh][16], then Im at sg + gim
-  const int gim = T * Lh * kNPad;
+  const int gim = T * LS * kNPad;
   double2* ys = reinterpret_cast<double2*>(sg);                     // P2 staging (FP64)
   double* fs = reinterpret_cast<double*>(smem + lay.g + (size_t)Lh * kChunk * sizeof(double2));
   double* dnl = reinterpret_cast<double*>(smem + lay.dnl);
@@ -919,7 +922,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       for (int e = 0; e < kEPT; ++e) {
         const int idx = tid + e * kBlock;
         const int lmh = idx >> 4;
-        if (lmh < Lh) sa[(t * Lh + lmh) * kNPad + (idx & 15)] = Rc{(R)accr[e], (R)acci[e]};
+        if (lmh < Lh) sa[(t * LS + lmh) * kNPad + (idx & 15)] = Rc{(R)accr[e], (R)acci[e]};
       }
     }
     MLIPG_STAMP(1)
@@ -933,7 +936,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       for (int u = warp; u < nNL; u += kBlock / 32) {
         const DeviceUnit un = A.nl_units[nl0 + u];
         R dsum = R(0);
-        dispatch_unit<false>(un, A.terms, sa, sg, gim, Lh, n, half, act, R(0), dsum);
+        dispatch_unit<false, LS>(un, A.terms, sa, sg, gim, n, half, act, R(0), dsum);
         dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
         if (half == 0) dnl[u * kNPad + n] = act ? (double)dsum : 0.0;
       }
@@ -986,11 +989,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         const DeviceIrrUnit iu = A.iunits[i0 + u];
         if (iu.nterm == 0) continue;   // padding of a balanced schedule
         if (T == 3)
-          dispatch_irr<3>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, Lh, n, half, act, eacc);
+          dispatch_irr<3, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, n, half, act, eacc);
         else if (T == 2)
-          dispatch_irr<2>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, Lh, n, half, act, eacc);
+          dispatch_irr<2, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, n, half, act, eacc);
         else
-          dispatch_irr<1>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, Lh, n, half, act, eacc);
+          dispatch_irr<1, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, n, half, act, eacc);
       }
       MLIPG_STAMP(3)   // warp 0's batched units (the warps' shares are balanced)
       for (int u = warp; u < nU; u += kBlock / 32) {
@@ -1002,7 +1005,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           if (un.nl_slot >= 0) hv += hnl[un.nl_slot * kNPad + n];
         }
         R dsum = R(0);
-        dispatch_unit<true>(un, A.terms, sa, sg, gim, Lh, n, half, act, (R)hv, dsum);
+        dispatch_unit<true, LS>(un, A.terms, sa, sg, gim, n, half, act, (R)hv, dsum);
         dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
         if (half == 0 && act) eacc += hv * (double)dsum;
       }
@@ -1030,7 +1033,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         R f[4], fd[4];
         radial4(A.radial, F, n0, (R)r, rc, f, fd);
         const double ir = 1.0 / r;
-        ForceVis v{sg + (size_t)tj * Lh * kNPad + n0, gim, f, fd, (R)(dx * ir), (R)(dy * ir),
+        ForceVis v{sg + (size_t)tj * LS * kNPad + n0, gim, f, fd, (R)(dx * ir), (R)(dy * ir),
                    (R)(dz * ir), R(0), R(0), R(0)};
         sh_visit<LCAP, true>((R)dx, (R)dy, (R)dz, (R)r, L, v);
         double fx = v.fx, fy = v.fy, fz = v.fz;
@@ -1104,8 +1107,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
   }
 }
 
-size_t smem_bytes(int T, int Lh, int nb_cap, int nl_cap) {
-  return smem_layout(T, Lh, nb_cap, nl_cap).total;
+size_t smem_bytes(int T, int L, int nb_cap, int nl_cap) {
+  const int lcap = L <= 6 ? 6 : (L <= 12 ? 12 : (L <= 16 ? 16 : 20));   // launch()'s pick
+  return smem_layout(T, (lcap + 1) * (lcap + 2) / 2, nb_cap, nl_cap).total;
 }
 
 template <int LCAP>
@@ -1127,6 +1131,7 @@ static int occupancy(size_t smem) {
 int max_blocks(int L, size_t smem) {
   if (L <= 6) return occupancy<6>(smem);
   if (L <= 12) return occupancy<12>(smem);
+  if (L <= 16) return occupancy<16>(smem);
   return occupancy<20>(smem);
 }
 
@@ -1138,6 +1143,9 @@ cudaError_t launch(int L, const KernelArgs& a, int grid, size_t smem, cudaStream
   } else if (L <= 12) {
     if ((e = prepare<12>(smem)) != cudaSuccess) return e;
     fused_kernel<12><<<grid, kBlock, smem, s>>>(a);
+  } else if (L <= 16) {
+    if ((e = prepare<16>(smem)) != cudaSuccess) return e;
+    fused_kernel<16><<<grid, kBlock, smem, s>>>(a);
   } else {
     if ((e = prepare<20>(smem)) != cudaSuccess) return e;
     fused_kernel<20><<<grid, kBlock, smem, s>>>(a);

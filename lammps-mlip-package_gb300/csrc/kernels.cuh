@@ -56,7 +56,7 @@ struct KernelArgs {
   unsigned long long* phase_clocks;  // optional [8]: SM cycles spent per phase (P1..P6)
 };
 
-size_t fused_smem_bytes(bool fp64, int T, int Lh, int nb_cap, int nl_cap);
+size_t fused_smem_bytes(bool fp64, int T, int L, int nb_cap, int nl_cap);
 int fused_max_blocks_per_sm(bool fp64, int L, size_t smem);
 cudaError_t launch_fused(bool fp64, int L, const KernelArgs& a, int grid, size_t smem,
                          cudaStream_t s);
@@ -68,7 +68,7 @@ cudaError_t init_device_constants();
 namespace mlipg {
 #define MLIPG_DECL_PREC(tag)                                                           \
   namespace tag {                                                                      \
-  size_t smem_bytes(int T, int Lh, int nb_cap, int nl_cap);                            \
+  size_t smem_bytes(int T, int L, int nb_cap, int nl_cap);                               \
   int max_blocks(int L, size_t smem);                                                  \
   cudaError_t launch(int L, const KernelArgs& a, int grid, size_t smem, cudaStream_t s); \
   cudaError_t init_constants();                                                        \

@@ -8,8 +8,8 @@ static_assert(kBlock / 32 == kCtaWarps, "schedules are dealt to the CTA's warps"
 static_assert(sizeof(DeviceUnit) == 32, "DeviceUnit must be 32 bytes");
 static_assert(sizeof(DevicePoly) == 32, "DevicePoly must be 32 bytes");
 
-size_t fused_smem_bytes(bool fp64, int T, int Lh, int nb_cap, int nl_cap) {
-  return fp64 ? f64::smem_bytes(T, Lh, nb_cap, nl_cap) : f32::smem_bytes(T, Lh, nb_cap, nl_cap);
+size_t fused_smem_bytes(bool fp64, int T, int L, int nb_cap, int nl_cap) {
+  return fp64 ? f64::smem_bytes(T, L, nb_cap, nl_cap) : f32::smem_bytes(T, L, nb_cap, nl_cap);
 }
 
 int fused_max_blocks_per_sm(bool fp64, int L, size_t smem) {
