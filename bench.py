@@ -43,6 +43,8 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "lammps-mlip-package_gb300"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
+from mlipg import replicas  # noqa: E402
+
 METRIC = "atom-steps/s E+F, mixed vs FP64 at force RMS err≤1e-4 eV/Å; p99 latency"
 UNIT = "atom-steps/s"
 
@@ -301,8 +303,7 @@ def run_ours(args, dist):
                          eatom=d_eat.data_ptr(), nb_cap=nb_cap)
 
     def barrier():
-        if dist["world"] > 1:
-            torch.distributed.barrier()
+        replicas.barrier(dist)
 
     for _ in range(args.warmup):
         step()
@@ -329,10 +330,7 @@ def run_ours(args, dist):
     ptot = max(sum(phases.values()), 1)
     phase_share = {k: round(v / ptot, 4) for k, v in phases.items()}
     el_max = el_ms
-    if dist["world"] > 1:
-        t = torch.tensor([el_ms], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el_max = float(t.item())
+    el_max = replicas.max_over_ranks(el_ms, dist)
     value = ncent_main * args.steps * dist["world"] / (el_max * 1e-3)
     e_mixed = float(d_out[0].item())
     if args.device_only:
@@ -376,10 +374,7 @@ def run_ours(args, dist):
     for _ in range(args.steps):
         e2e_step()
     e2e_el = time.perf_counter() - t0
-    if dist["world"] > 1:
-        t = torch.tensor([e2e_el], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_el = float(t.item())
+    e2e_el = replicas.max_over_ranks(e2e_el, dist)
     e2e = {"value": natoms * args.steps * dist["world"] / e2e_el, "unit": UNIT,
            "h2d_bytes_per_step": int(32 * sysm.nall + 4 * natoms + 4 * (natoms + 1) +
                                      4 * sysm.npairs),
@@ -543,10 +538,7 @@ def run_batch(args, dist):
         c = clocks.stop()
         g.set_profiling(False)
         el = ev0.elapsed_time(ev1)
-        if dist["world"] > 1:
-            t = torch.tensor([el], dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            el = float(t.item())
+        el = replicas.max_over_ranks(el, dist)
         rates[prec] = natoms * args.steps * dist["world"] / (el * 1e-3)
         kt = [t for t in g.kernel_times() if t > 0]
         kms[prec] = float(np.mean(kt)) if kt else float("nan")
@@ -738,10 +730,7 @@ def run_md(args, dist):
     el = time.perf_counter() - t0
     clk = clocks.stop()
     th1 = md.thermo()
-    if dist["world"] > 1:
-        t = torch.tensor([el], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el = float(t.item())
+    el = replicas.max_over_ranks(el, dist)
     n = cell.natoms
     value = n * args.steps * dist["world"] / el
     nb = 4 * 4.0 / 3.0 * np.pi * 6.0 ** 3 / spec["a"] ** 3
@@ -800,13 +789,7 @@ def main():
     args = ap.parse_args()
     if args.tiling:
         args.autotune = False
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    dist = {"world": world, "rank": rank}
-    if world > 1:
-        import torch.distributed
-        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        torch.distributed.init_process_group("gloo")
+    dist = replicas.init("gloo")
     try:
         kind = WORKLOADS[args.workload].get("kind", "cell")
         if args.impl == "reference":
@@ -820,9 +803,7 @@ def main():
         else:
             run_ours(args, dist)
     finally:
-        if world > 1:
-            import torch.distributed
-            torch.distributed.destroy_process_group()
+        replicas.finish(dist)
 
 
 if __name__ == "__main__":
