@@ -161,6 +161,19 @@ def cpu_baseline(pot_path, sysm, seconds=15.0, seed=0):
                       "(energy, adjoint, pair forces; %.1f s)" % (len(centres), sysm.nlocal, t)}
 
 
+def profiled_traffic(workload):
+    """DRAM bytes (read + write) of one full launch of the fused kernel, from
+    the ncu summary committed for this workload (`traffic_bytes_per_launch:`
+    line)."""
+    import re
+    path = os.path.join(REPO, "profiles", "fused_kernel_%s.md" % workload)
+    if not os.path.exists(path):
+        return {"traffic": None}
+    m = re.search(r"^traffic_bytes_per_launch:\s*(\d+)", open(path).read(), re.M)
+    return {"traffic": int(m.group(1)) if m else None,
+            "traffic_source": os.path.relpath(path, REPO)}
+
+
 def mean_neighbours_in_cutoff(sysm, rc):
     d = sysm.x[sysm.nbr_idx] - np.repeat(sysm.x[:sysm.nlocal], np.diff(sysm.nbr_off), axis=0)
     inside = np.einsum("ij,ij->i", d, d) <= rc * rc
@@ -421,11 +434,11 @@ def run_ours(args, dist):
                            "the machine's measured peaks cover HBM copy and bf16 tensor only",
             "kernel": "fused_kernel<12> (mixed)", "kernel_ms": kmean,
             "algorithmic_flops_per_launch": flops,
-            "flops_per_atom": flops / natoms}
-    prof = os.path.join(REPO, "profiles", "traffic_" + args.workload + ".json")
-    if os.path.exists(prof):
-        with open(prof) as f:
-            roof["traffic"] = json.load(f).get("dram_bytes_per_launch")
+            "flops_per_atom": flops / natoms,
+            # positions+element, centre, CSR offsets and indices read; forces written
+            "algorithmic_bytes_per_launch": int(32 * sysm.nall + 8 * natoms + 4 * sysm.npairs +
+                                                24 * sysm.nall)}
+    roof.update(profiled_traffic(args.workload))
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist["world"],
