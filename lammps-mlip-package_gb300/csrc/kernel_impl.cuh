@@ -564,9 +564,19 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
   const int s0 = (int)u.s0;
   constexpr int es = Lh * kNPad;   // element stride in the a / G arrays
   R eu = R(0);
-  const int kend = u.term0 + u.nterm;
-  for (int k = u.term0 + half; k < kend; k += 2) {
-    const int4 raw = __ldg(reinterpret_cast<const int4*>(terms + k));
+  // the two half-warps take alternate terms; the adjoints of slot z (and of
+  // the fixed slot 0 of order 4) are kept in registers while a half-warp's
+  // consecutive terms address the same order parameter (runs of the table's
+  // outer m loops) and flushed when its next term moves on
+  const int ke = u.term0 + u.nterm, kb = u.term0 + half;
+  R azr[NZ], azi[NZ], a0r = R(0), a0i = R(0);
+#pragma unroll
+  for (int z = 0; z < NZ; ++z) { azr[z] = R(0); azi[z] = R(0); }
+  int4 nxt = kb < ke ? __ldg(reinterpret_cast<const int4*>(terms + kb)) : make_int4(0, 0, 0, 0);
+  for (int k = kb; k < ke; k += 2) {
+    const int4 raw = nxt;
+    if (k + 2 < ke) nxt = __ldg(reinterpret_cast<const int4*>(terms + k + 2));
+    const bool last = k + 2 >= ke;
     const R c = (R)__hiloint2double(raw.y, raw.x);
     const unsigned lw = (unsigned)raw.z, code = ((unsigned)raw.w) >> 16;
     const bool self = (code >> 12) & 1u;
@@ -684,17 +694,41 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
 #pragma unroll
         for (int y = 0; y < NY; ++y) flush(PY, y, gyr[y], gyi[y]);
       }
-      if (Q >= 3) {
+    }
+    if (Q >= 3) {   // slot z: A S_z, accumulated over the run
+      const unsigned cd = (code >> (2 * PZ)) & 3u;
+      const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
+      const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
 #pragma unroll
-        for (int z = 0; z < NZ; ++z) flush(PZ, z, gzr[z], gzi[z]);
+      for (int z = 0; z < NZ; ++z) {
+        azr[z] += kr * (Ar * gzr[z] - Ai * gzi[z]);
+        azi[z] += ki * (Ar * gzi[z] + Ai * gzr[z]);
       }
-      if (Q == 4) {   // slot 0: S, without the prefix A (it is slot 0's own factor)
-        const unsigned cd = code & 3u;
-        const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
-        const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
-        R* gp = sg + s0 * es + lo[0];
-        atomicAdd(gp, kr * Sr);
-        if (cd < 2u) atomicAdd(gp + gim, ki * Si);
+      if (last || ((((unsigned)nxt.z ^ lw) >> (8 * PZ)) & 255u) != 0u) {
+        if (act) {
+#pragma unroll
+          for (int z = 0; z < NZ; ++z) {
+            R* gp = sg + z * es + lo[PZ];
+            atomicAdd(gp, azr[z]);
+            atomicAdd(gp + gim, azi[z]);
+          }
+        }
+#pragma unroll
+        for (int z = 0; z < NZ; ++z) { azr[z] = R(0); azi[z] = R(0); }
+      }
+    }
+    if (Q == 4) {   // slot 0: S, without the prefix A (it is slot 0's own factor)
+      const unsigned cd = code & 3u;
+      a0r += ((cd == (unsigned)kSlotMZero) ? R(2) * c : c) * Sr;
+      a0i += ((cd == 0u) ? c : (cd == 1u ? -c : R(0))) * Si;
+      if (last || (((unsigned)nxt.z ^ lw) & 255u) != 0u) {
+        if (act) {
+          R* gp = sg + s0 * es + lo[0];
+          atomicAdd(gp, a0r);
+          atomicAdd(gp + gim, a0i);
+        }
+        a0r = R(0);
+        a0i = R(0);
       }
     }
   }
