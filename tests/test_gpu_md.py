@@ -81,6 +81,15 @@ def test_graph_equals_eager_and_rebuilds_keep_physics(potdir):
 
 
 def test_nve_energy_conservation_mixed(potdir):
-    x0, t0 = run_nve(potdir["gtinv-820"], 1, 0.001, prec=mlipg.PREC_MIXED)
-    x1, t1 = run_nve(potdir["gtinv-820"], 200, 0.001, prec=mlipg.PREC_MIXED)
-    assert abs(t1["etotal"] - t0["etotal"]) / 32 < 2e-5
+    """Velocity Verlet itself moves the total energy of this cell by ~1e-5
+    eV/atom per 100 steps (the reference's own FP64 log: TotEng -135.40507 ->
+    -135.40539), so the mixed run's drift is compared with the FP64 run's:
+    the FP32 adjoint products may add no more than the integrator's own drift
+    scale, 2e-5 eV/atom over 200 steps (measured: ~6e-6)."""
+    drift = {}
+    for prec in (mlipg.PREC_FP64, mlipg.PREC_MIXED):
+        _, t0 = run_nve(potdir["gtinv-820"], 1, 0.001, prec=prec)
+        _, t1 = run_nve(potdir["gtinv-820"], 200, 0.001, prec=prec)
+        drift[prec] = (t1["etotal"] - t0["etotal"]) / 32
+    assert abs(drift[mlipg.PREC_MIXED] - drift[mlipg.PREC_FP64]) < 2e-5
+    assert abs(drift[mlipg.PREC_FP64]) < 5e-5
