@@ -347,11 +347,13 @@ __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* 
         }
         const unsigned cd = (code >> (2 * p)) & 3u;
         const R kr = (cd == (unsigned)kSlotMZero) ? R(2) : R(1);
-        if (act) {
-          R* gp = sg + off[p] + lmh[p] * kNPad;
-          atomicAdd(gp, cc * kr * Pr);
-          if (cd < 2u) atomicAdd(gp + gim, (cd == 0u ? cc : -cc) * Pi);
-        }
+        const R ki = (cd == 0u) ? R(1) : (cd == 1u ? R(-1) : R(0));
+        // unconditional: lanes n >= F and unused imaginary parts add exact
+        // zeros (to padding entries / entries nothing reads), which keeps the
+        // flush free of divergent branches
+        R* gp = sg + off[p] + lmh[p] * kNPad;
+        atomicAdd(gp, cc * kr * Pr);
+        atomicAdd(gp + gim, cc * ki * Pi);
       }
     }
   }
@@ -492,32 +494,32 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
       for (int s2 = 0; s2 < TT; ++s2) et += gr[2][s2] * ar[2][s2] - gi[2][s2] * ai[2][s2];
       eu += ce * et;
     }
-    if (act) {
+    // unconditional flush (zeros from lanes n >= F and unused imaginary parts)
 #pragma unroll
-      for (int p = 0; p < Q; ++p) {
-        const unsigned cd = (code >> (2 * p)) & 3u;
-        const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
-        const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
-        if (p == 0) {
+    for (int p = 0; p < Q; ++p) {
+      const unsigned cd = (code >> (2 * p)) & 3u;
+      const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
+      const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
+      if (p == 0) {
 #pragma unroll
-          for (int s = 0; s < N0; ++s) {
-            R* gp = sg + (s0base + s) * es + lo[0];
-            atomicAdd(gp, kr * g0r[s]);
-            if (cd < 2u) atomicAdd(gp + gim, ki * g0i[s]);
-          }
-        } else {
+        for (int s = 0; s < N0; ++s) {
+          R* gp = sg + (s0base + s) * es + lo[0];
+          atomicAdd(gp, kr * g0r[s]);
+          atomicAdd(gp + gim, ki * g0i[s]);
+        }
+      } else {
 #pragma unroll
-          for (int s = 0; s < TT; ++s) {
-            R* gp = sg + s * es + lo[p];
-            atomicAdd(gp, kr * gr[p][s]);
-            if (cd < 2u) atomicAdd(gp + gim, ki * gi[p][s]);
-          }
+        for (int s = 0; s < TT; ++s) {
+          R* gp = sg + s * es + lo[p];
+          atomicAdd(gp, kr * gr[p][s]);
+          atomicAdd(gp + gim, ki * gi[p][s]);
         }
       }
     }
   }
-  // this half-warp's terms, in REAL, into the centre's FP64 energy
-  if (act) eacc += (double)eu;
+  // this half-warp's terms, in REAL, into the centre's FP64 energy (zero on
+  // lanes n >= F)
+  eacc += (double)eu;
 }
 
 // Element tuples of one irreps (order Q <= 4, TT elements) over a chunk of
@@ -678,15 +680,17 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       }
     }
     eu += ce * (Ar * Sr - Ai * Si);
-    if (act) {
-      // adjoint of slot p: A * partial, scaled by (kr, ki) from its storage code
+    {
+      // adjoint of slot p: A * partial, scaled by (kr, ki) from its storage
+      // code; unconditional (lanes n >= F and unused imaginary parts add
+      // exact zeros), so the flush has no divergent branches
       const auto flush = [&](int p, int e, R vr, R vi) {
         const unsigned cd = (code >> (2 * p)) & 3u;
         const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
         const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
         R* gp = sg + e * es + lo[p];
         atomicAdd(gp, kr * (Ar * vr - Ai * vi));
-        if (cd < 2u) atomicAdd(gp + gim, ki * (Ar * vi + Ai * vr));
+        atomicAdd(gp + gim, ki * (Ar * vi + Ai * vr));
       };
 #pragma unroll
       for (int x = 0; x < NX; ++x) flush(PX, x, gxr[x], gxi[x]);
@@ -704,14 +708,15 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
         azr[z] += kr * (Ar * gzr[z] - Ai * gzi[z]);
         azi[z] += ki * (Ar * gzi[z] + Ai * gzr[z]);
       }
-      if (last || ((((unsigned)nxt.z ^ lw) >> (8 * PZ)) & 255u) != 0u) {
-        if (act) {
+      // flush when this half-warp's next term moves on; voted so that both
+      // halves take the (then uniform) branch together
+      const bool need = last || ((((unsigned)nxt.z ^ lw) >> (8 * PZ)) & 255u) != 0u;
+      if (__any_sync(__activemask(), need)) {
 #pragma unroll
-          for (int z = 0; z < NZ; ++z) {
-            R* gp = sg + z * es + lo[PZ];
-            atomicAdd(gp, azr[z]);
-            atomicAdd(gp + gim, azi[z]);
-          }
+        for (int z = 0; z < NZ; ++z) {
+          R* gp = sg + z * es + lo[PZ];
+          atomicAdd(gp, azr[z]);
+          atomicAdd(gp + gim, azi[z]);
         }
 #pragma unroll
         for (int z = 0; z < NZ; ++z) { azr[z] = R(0); azi[z] = R(0); }
@@ -721,19 +726,19 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       const unsigned cd = code & 3u;
       a0r += ((cd == (unsigned)kSlotMZero) ? R(2) * c : c) * Sr;
       a0i += ((cd == 0u) ? c : (cd == 1u ? -c : R(0))) * Si;
-      if (last || (((unsigned)nxt.z ^ lw) & 255u) != 0u) {
-        if (act) {
-          R* gp = sg + s0 * es + lo[0];
-          atomicAdd(gp, a0r);
-          atomicAdd(gp + gim, a0i);
-        }
+      const bool need0 = last || (((unsigned)nxt.z ^ lw) & 255u) != 0u;
+      if (__any_sync(__activemask(), need0)) {
+        R* gp = sg + s0 * es + lo[0];
+        atomicAdd(gp, a0r);
+        atomicAdd(gp + gim, a0i);
         a0r = R(0);
         a0i = R(0);
       }
     }
   }
-  // this half-warp's terms, in REAL, into the centre's FP64 energy
-  if (act) eacc += (double)eu;
+  // this half-warp's terms, in REAL, into the centre's FP64 energy (zero on
+  // lanes n >= F)
+  eacc += (double)eu;
 }
 
 template <int TT, int Lh>
