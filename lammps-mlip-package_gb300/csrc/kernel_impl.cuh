@@ -522,6 +522,14 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
   eacc += (double)eu;
 }
 
+// acc += a * b (complex) as two fused multiply-add chains
+__device__ __forceinline__ void cmac(R& accr, R& acci, R ar, R ai, R br, R bi) {
+  accr = fma(ar, br, accr);
+  accr = fma(-ai, bi, accr);
+  acci = fma(ar, bi, acci);
+  acci = fma(ai, br, acci);
+}
+
 // Element tuples of one irreps (order Q <= 4, TT elements) over a chunk of
 // canonical terms.  Order 4 fixes the element of slot 0 per unit (u.s0; its
 // order parameter is the prefix A); the last three slots z, x, y (the last
@@ -643,8 +651,8 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
           R tr = R(0), ti = R(0);
 #pragma unroll
           for (int y = 0; y < NY; ++y) {
-            tr += H[z][x][y] * cr[y];
-            ti += H[z][x][y] * ci[y];
+            tr = fma(H[z][x][y], cr[y], tr);
+            ti = fma(H[z][x][y], ci[y], ti);
           }
           mr[x] = tr;
           mi[x] = ti;
@@ -653,17 +661,14 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       R szr = R(0), szi = R(0);
 #pragma unroll
       for (int x = 0; x < NX; ++x) {
-        szr += br[x] * mr[x] - bi[x] * mi[x];
-        szi += br[x] * mi[x] + bi[x] * mr[x];
+        cmac(szr, szi, br[x], bi[x], mr[x], mi[x]);
       }
       gzr[z] = szr;
       gzi[z] = szi;
-      Sr += zr[z] * szr - zi[z] * szi;
-      Si += zr[z] * szi + zi[z] * szr;
+      cmac(Sr, Si, zr[z], zi[z], szr, szi);
 #pragma unroll
       for (int x = 0; x < NX; ++x) {
-        gxr[x] += zr[z] * mr[x] - zi[z] * mi[x];
-        gxi[x] += zr[z] * mi[x] + zi[z] * mr[x];
+        cmac(gxr[x], gxi[x], zr[z], zi[z], mr[x], mi[x]);
       }
       if (Q > 1) {
 #pragma unroll
@@ -671,11 +676,10 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
           R tr = R(0), ti = R(0);
 #pragma unroll
           for (int x = 0; x < NX; ++x) {
-            tr += H[z][x][y] * br[x];
-            ti += H[z][x][y] * bi[x];
+            tr = fma(H[z][x][y], br[x], tr);
+            ti = fma(H[z][x][y], bi[x], ti);
           }
-          gyr[y] += zr[z] * tr - zi[z] * ti;
-          gyi[y] += zr[z] * ti + zi[z] * tr;
+          cmac(gyr[y], gyi[y], zr[z], zi[z], tr, ti);
         }
       }
     }
