@@ -375,6 +375,7 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.nb_cap = nb_cap;
   a.nl_cap = nl_cap;
   a.rc = M.pot.cutoff;
+  a.g_bound = (float)M.g_bound;
   a.f = f;
   a.eatom = eatom;
   a.vatom = vatom;
@@ -530,6 +531,8 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
     return fail(h, MLIPG_ECAPACITY, "an atom has more than %d neighbours inside the cutoff",
                 std::max(32, std::min(kNbCapMax, (maxn + 31) / 32 * 32)));
   if (status & kStatusBadType) return fail(h, MLIPG_EINVAL, "element index out of range");
+  if (status & kStatusAdjointRange)
+    return fail(h, MLIPG_ENOTSUP, "adjoint values outside the mixed path's fixed-point range");
   const double* hf = h->h_f.as<double>();
   const long long nf = (long long)nall * 3;
 #pragma omp parallel for schedule(static)
@@ -819,6 +822,7 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
   a.nb_cap = nb_cap;
   a.nl_cap = nl_cap;
   a.rc = M.pot.cutoff;
+  a.g_bound = (float)M.g_bound;
   a.f = d_f;
   a.eatom = d_eatom;
   a.vatom = d_vatom;

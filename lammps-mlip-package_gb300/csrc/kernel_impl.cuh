@@ -287,10 +287,39 @@ __device__ __forceinline__ void pair_disp(const KernelArgs& A, int c, int k, con
 }
 
 // One coupling unit for all n: warp halves take alternate terms.
+// Adjoint accumulation into shared memory.  FP64: double atomics.  Mixed
+// path: exact 64-bit fixed point with native 32-bit integer atomics (a
+// shared-memory FP32 atomic add is a compare-and-swap loop, six times slower).
+// Each flush is scaled by 2^e (e adapted per centre element) and split
+// exactly into a high part, a multiple of 2^16, and a low part of at most
+// 2^15 (both rounded by the exact magic-number add), which go to two int32
+// arrays (low part at p + lo_off); no carries are needed because the host
+// bounds the flushes per entry.  Sums are exact and order independent; the
+// centre's largest |scaled flush| is tracked so that out-of-range flushes are
+// detected (the invariant phase is then redone at a smaller scale).
+struct GFix {
+  R scale;     // 2^e
+  R vmax;      // largest |scaled flush| of this thread
+  int lo_off;  // element offset of the low-part array (2 x the imaginary offset)
+};
+// y: the flush already multiplied by g.scale (1 in FP64); lo: element offset
+// of the low-part array (2 x the imaginary offset)
+__device__ __forceinline__ void gput(R* p, R y, GFix& g, int lo) {
+  if constexpr (sizeof(R) == 4) {
+    g.vmax = fmaxf(g.vmax, fabsf(y));
+    const float th = fmaf(y, 1.0f / 65536.0f, 12582912.0f);   // rint(y / 2^16) + 1.5 * 2^23
+    const float yl = fmaf(-(th - 12582912.0f), 65536.0f, y);  // y - hi * 2^16, exact
+    atomicAdd(reinterpret_cast<int*>(p), __float_as_int(th) - 0x4B400000);
+    atomicAdd(reinterpret_cast<int*>(p) + lo, __float_as_int(yl + 12582912.0f) - 0x4B400000);
+  } else {
+    atomicAdd(p, y);
+  }
+}
+
 template <int Q, bool WITH_G, int Lh>
 __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* __restrict__ terms,
-                                         const Rc* sa, R* sg, int gim, int n, int half,
-                                         bool act, R H, R& dsum) {
+                                         const Rc* sa, R* sg, int gim, GFix& gf, int n,
+                                         int half, bool act, R H, R& dsum) {
   int off[Q];
 #pragma unroll
   for (int p = 0; p < Q; ++p) off[p] = (int)u.s[p] * Lh * kNPad + n;
@@ -352,8 +381,9 @@ __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* 
         // zeros (to padding entries / entries nothing reads), which keeps the
         // flush free of divergent branches
         R* gp = sg + off[p] + lmh[p] * kNPad;
-        atomicAdd(gp, cc * kr * Pr);
-        atomicAdd(gp + gim, cc * ki * Pi);
+        const R cs = cc * gf.scale;
+        gput(gp, cs * kr * Pr, gf, gf.lo_off);
+        gput(gp + gim, cs * ki * Pi, gf, gf.lo_off);
       }
     }
   }
@@ -377,8 +407,8 @@ template <int Q, int TT, int Lh>
 __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
                                         const R* __restrict__ wlin, const double* hnl,
-                                        const Rc* sa, R* sg, int gim, int n, int half,
-                                        bool act, double& eacc) {
+                                        const Rc* sa, R* sg, int gim, GFix& gf, int n,
+                                        int half, bool act, double& eacc) {
   constexpr int N0 = TT;                                  // elements of slot 0
   constexpr int NT = (Q == 1) ? N0 : (Q == 2 ? N0 * TT : N0 * TT * TT);
   constexpr int s0base = 0;
@@ -398,6 +428,7 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
   // the nonlinear part sum hnl d of H is subtracted once per centre.
   R eu = R(0);
   constexpr int es = Lh * kNPad;   // element stride in the a / G arrays
+  constexpr int kIm = TT * es, kLo = 2 * kIm;   // imaginary / low-part offsets (T == TT)
   const int kend = u.term0 + u.nterm;
   for (int k = u.term0 + half; k < kend; k += 2) {
     const int4 raw = __ldg(reinterpret_cast<const int4*>(terms + k));
@@ -498,21 +529,22 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
 #pragma unroll
     for (int p = 0; p < Q; ++p) {
       const unsigned cd = (code >> (2 * p)) & 3u;
-      const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
-      const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
+      const R cs = c * gf.scale;
+      const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * cs : cs;
+      const R ki = (cd == 0u) ? cs : (cd == 1u ? -cs : R(0));
       if (p == 0) {
 #pragma unroll
         for (int s = 0; s < N0; ++s) {
           R* gp = sg + (s0base + s) * es + lo[0];
-          atomicAdd(gp, kr * g0r[s]);
-          atomicAdd(gp + gim, ki * g0i[s]);
+          gput(gp, kr * g0r[s], gf, kLo);
+          gput(gp + kIm, ki * g0i[s], gf, kLo);
         }
       } else {
 #pragma unroll
         for (int s = 0; s < TT; ++s) {
           R* gp = sg + s * es + lo[p];
-          atomicAdd(gp, kr * gr[p][s]);
-          atomicAdd(gp + gim, ki * gi[p][s]);
+          gput(gp, kr * gr[p][s], gf, kLo);
+          gput(gp + kIm, ki * gi[p][s], gf, kLo);
         }
       }
     }
@@ -547,8 +579,8 @@ template <int Q, int TT, int Lh>
 __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
                                         const R* __restrict__ wlin, const double* hnl,
-                                        const Rc* sa, R* sg, int gim, int n, int half,
-                                        bool act, double& eacc) {
+                                        const Rc* sa, R* sg, int gim, GFix& gf, int n,
+                                        int half, bool act, double& eacc) {
   constexpr int NZ = (Q >= 3) ? TT : 1;      // elements of slot z
   constexpr int NX = TT;                     // elements of slot x (slot 0 for Q = 1)
   constexpr int NY = (Q == 1) ? 1 : TT;      // elements of slot y
@@ -573,6 +605,7 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       }
   const int s0 = (int)u.s0;
   constexpr int es = Lh * kNPad;   // element stride in the a / G arrays
+  constexpr int kIm = TT * es, kLo = 2 * kIm;   // imaginary / low-part offsets (T == TT)
   R eu = R(0);
   // the two half-warps take alternate terms; the adjoints of slot z (and of
   // the fixed slot 0 of order 4) are kept in registers while a half-warp's
@@ -688,13 +721,14 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       // adjoint of slot p: A * partial, scaled by (kr, ki) from its storage
       // code; unconditional (lanes n >= F and unused imaginary parts add
       // exact zeros), so the flush has no divergent branches
+      const R cs = c * gf.scale;
       const auto flush = [&](int p, int e, R vr, R vi) {
         const unsigned cd = (code >> (2 * p)) & 3u;
-        const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
-        const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
+        const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * cs : cs;
+        const R ki = (cd == 0u) ? cs : (cd == 1u ? -cs : R(0));
         R* gp = sg + e * es + lo[p];
-        atomicAdd(gp, kr * (Ar * vr - Ai * vi));
-        atomicAdd(gp + gim, ki * (Ar * vi + Ai * vr));
+        gput(gp, kr * (Ar * vr - Ai * vi), gf, kLo);
+        gput(gp + kIm, ki * (Ar * vi + Ai * vr), gf, kLo);
       };
 #pragma unroll
       for (int x = 0; x < NX; ++x) flush(PX, x, gxr[x], gxi[x]);
@@ -705,8 +739,9 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
     }
     if (Q >= 3) {   // slot z: A S_z, accumulated over the run
       const unsigned cd = (code >> (2 * PZ)) & 3u;
-      const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * c : c;
-      const R ki = (cd == 0u) ? c : (cd == 1u ? -c : R(0));
+      const R cs = c * gf.scale;
+      const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * cs : cs;
+      const R ki = (cd == 0u) ? cs : (cd == 1u ? -cs : R(0));
 #pragma unroll
       for (int z = 0; z < NZ; ++z) {
         azr[z] += kr * (Ar * gzr[z] - Ai * gzi[z]);
@@ -719,8 +754,8 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
 #pragma unroll
         for (int z = 0; z < NZ; ++z) {
           R* gp = sg + z * es + lo[PZ];
-          atomicAdd(gp, azr[z]);
-          atomicAdd(gp + gim, azi[z]);
+          gput(gp, azr[z], gf, kLo);
+          gput(gp + kIm, azi[z], gf, kLo);
         }
 #pragma unroll
         for (int z = 0; z < NZ; ++z) { azr[z] = R(0); azi[z] = R(0); }
@@ -728,13 +763,14 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
     }
     if (Q == 4) {   // slot 0: S, without the prefix A (it is slot 0's own factor)
       const unsigned cd = code & 3u;
-      a0r += ((cd == (unsigned)kSlotMZero) ? R(2) * c : c) * Sr;
-      a0i += ((cd == 0u) ? c : (cd == 1u ? -c : R(0))) * Si;
+      const R cs = c * gf.scale;
+      a0r += ((cd == (unsigned)kSlotMZero) ? R(2) * cs : cs) * Sr;
+      a0i += ((cd == 0u) ? cs : (cd == 1u ? -cs : R(0))) * Si;
       const bool need0 = last || (((unsigned)nxt.z ^ lw) & 255u) != 0u;
       if (__any_sync(__activemask(), need0)) {
         R* gp = sg + s0 * es + lo[0];
-        atomicAdd(gp, a0r);
-        atomicAdd(gp + gim, a0i);
+        gput(gp, a0r, gf, kLo);
+        gput(gp + kIm, a0i, gf, kLo);
         a0r = R(0);
         a0i = R(0);
       }
@@ -749,34 +785,34 @@ template <int TT, int Lh>
 __device__ __forceinline__ void dispatch_irr(const DeviceIrrUnit& u, const DeviceTuple* tups,
                                              const DeviceTerm* terms, const R* wlin,
                                              const double* hnl, const Rc* sa, R* sg, int gim,
-                                             int n, int half, bool act, double& eacc) {
+                                             GFix& gf, int n, int half, bool act, double& eacc) {
   if (TT <= 2 && u.q <= 3) {
     switch (u.q) {
-      case 1: run_irr_direct<1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
-      case 2: run_irr_direct<2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
-      default: run_irr_direct<3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
+      case 1: run_irr_direct<1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+      case 2: run_irr_direct<2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+      default: run_irr_direct<3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
     }
     return;
   }
   switch (u.q) {
-    case 1: run_irr<1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
-    case 2: run_irr<2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
-    case 3: run_irr<3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
-    default: run_irr<4, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, n, half, act, eacc); break;
+    case 1: run_irr<1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+    case 2: run_irr<2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+    case 3: run_irr<3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+    default: run_irr<4, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
   }
 }
 
 template <bool WITH_G, int Lh>
 __device__ __forceinline__ void dispatch_unit(const DeviceUnit& u, const DeviceTerm* terms,
-                                              const Rc* sa, R* sg, int gim, int n,
+                                              const Rc* sa, R* sg, int gim, GFix& gf, int n,
                                               int half, bool act, R H, R& dsum) {
   switch (u.q) {
-    case 1: run_unit<1, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
-    case 2: run_unit<2, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
-    case 3: run_unit<3, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
-    case 4: run_unit<4, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
-    case 5: run_unit<5, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
-    default: run_unit<6, WITH_G, Lh>(u, terms, sa, sg, gim, n, half, act, H, dsum); break;
+    case 1: run_unit<1, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    case 2: run_unit<2, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    case 3: run_unit<3, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    case 4: run_unit<4, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    case 5: run_unit<5, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    default: run_unit<6, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
   }
 }
 
@@ -791,10 +827,12 @@ struct SmemLayout {
 __host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int nl_cap) {
   SmemLayout s;
   const size_t an = (size_t)T * Lh * kNPad * sizeof(Rc);
+  // adjoint: FP64 re/im, or the mixed path's int32 high + low parts of re/im
+  const size_t gn = (size_t)T * Lh * kNPad * 16;
   const size_t stage = (size_t)Lh * kChunk * sizeof(double2) + (size_t)kChunk * kNPad * sizeof(double);
   s.a = 0;
   s.g = align16(an);
-  s.dnl = s.g + align16(an > stage ? an : stage);
+  s.dnl = s.g + align16(gn > stage ? gn : stage);
   s.hnl = s.dnl + align16((size_t)nl_cap * kNPad * sizeof(double));
   s.nbk = s.hnl + align16((size_t)nl_cap * kNPad * sizeof(double));
   s.misc = s.nbk + align16((size_t)nb_cap * sizeof(int));
@@ -839,6 +877,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     tstamp = t_;                                \
   }
 
+  // mixed path: fixed-point exponent of the adjoint per centre element
+  // (adapted from centre to centre; the first centre of an element adjusts it)
+  if (tid < kMaxTypes) misc[16 + tid] = 0;
+  __syncthreads();
   for (int c = blockIdx.x; c < A.ncenters; c += gridDim.x) {
     const int i = __ldg(A.centers + c);
     const double4 xi = A.x4[i];
@@ -979,7 +1021,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       for (int u = warp; u < nNL; u += kBlock / 32) {
         const DeviceUnit un = A.nl_units[nl0 + u];
         R dsum = R(0);
-        dispatch_unit<false, LS>(un, A.terms, sa, sg, gim, n, half, act, R(0), dsum);
+        GFix gnone{R(1), R(0), 0};
+        dispatch_unit<false, LS>(un, A.terms, sa, sg, gim, gnone, n, half, act, R(0), dsum);
         dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
         if (half == 0) dnl[u * kNPad + n] = act ? (double)dsum : 0.0;
       }
@@ -1015,13 +1058,21 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       }
     }
     // ---------------------------------------------------------------- P4
-    for (int e = tid; e < 2 * gim; e += kBlock) sg[e] = R(0);
-    __syncthreads();
     // P5 weighs every feature's products with H = w + dE_poly/dd: remove the
     // nonlinear part's share, sum hnl d over the nonlinear features
     for (int e = tid; e < nNL * kNPad; e += kBlock) eacc -= hnl[e] * dnl[e];
     MLIPG_STAMP(2)
     // ---------------------------------------------------------------- P5
+    // (mixed path: redone once at the measured scale if a flush left the
+    // fixed-point range; the energy of the failed attempt is discarded)
+    const double eacc0 = eacc;
+    int gexp = 0;
+    for (int attempt = 0;; ++attempt) {
+    for (int e = tid; e < (sizeof(R) == 4 ? 4 : 2) * gim; e += kBlock) sg[e] = R(0);
+    gexp = misc[16 + ti];
+    if (tid == 0) misc[12] = 0;
+    __syncthreads();   // G zeroed; everyone has read this attempt's scale
+    GFix gf{sizeof(R) == 4 ? (R)ldexpf(1.0f, gexp) : R(1), R(0), 2 * gim};
     {
       const int u0 = __ldg(A.unit_off + ti), nU = __ldg(A.unit_off + ti + 1) - u0;
       const int i0 = __ldg(A.iunit_off + ti), nI = __ldg(A.iunit_off + ti + 1) - i0;
@@ -1032,11 +1083,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         const DeviceIrrUnit iu = A.iunits[i0 + u];
         if (iu.nterm == 0) continue;   // padding of a balanced schedule
         if (T == 3)
-          dispatch_irr<3, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, n, half, act, eacc);
+          dispatch_irr<3, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, eacc);
         else if (T == 2)
-          dispatch_irr<2, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, n, half, act, eacc);
+          dispatch_irr<2, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, eacc);
         else
-          dispatch_irr<1, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, n, half, act, eacc);
+          dispatch_irr<1, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, eacc);
       }
       MLIPG_STAMP(3)   // warp 0's batched units (the warps' shares are balanced)
       for (int u = warp; u < nU; u += kBlock / 32) {
@@ -1048,12 +1099,49 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           if (un.nl_slot >= 0) hv += hnl[un.nl_slot * kNPad + n];
         }
         R dsum = R(0);
-        dispatch_unit<true, LS>(un, A.terms, sa, sg, gim, n, half, act, (R)hv, dsum);
+        dispatch_unit<true, LS>(un, A.terms, sa, sg, gim, gf, n, half, act, (R)hv, dsum);
         dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
         if (half == 0 && act) eacc += hv * (double)dsum;
       }
     }
+    if (sizeof(R) != 4) {
+      __syncthreads();
+      break;
+    }
+    {
+      // largest |scaled flush| of the CTA
+      float vm = (float)gf.vmax;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+      if (lane == 0) atomicMax(misc + 12, __float_as_int(vm));
+    }
     __syncthreads();
+    const float vm = __int_as_float(misc[12]);
+    const bool out = !(vm < A.g_bound);   // also true for NaN
+    // a scale that leaves more than 6 bits of the range unused is redone too
+    const bool coarse = vm > 0.0f && vm < A.g_bound * (1.0f / 64.0f);
+    if (tid == 0 && vm > 0.0f && vm < 3.0e38f) {
+      // next scale: the largest flush at half the bound
+      int lv = ilogbf(vm);
+      if (vm > ldexpf(1.0f, lv)) ++lv;
+      misc[16 + ti] = max(-120, min(120, gexp + ilogbf(A.g_bound) - 1 - lv));
+    }
+    if ((!out && !coarse) || attempt >= 2) {
+      if (out && tid == 0) atomicOr(A.status, kStatusAdjointRange);
+      break;
+    }
+    eacc = eacc0;
+    __syncthreads();   // misc[12] read by all before the next attempt resets it
+    }
+    if (sizeof(R) == 4) {
+      // fixed point -> float, in place
+      __syncthreads();
+      const float inv = ldexpf(1.0f, -gexp);
+      const int* gi = reinterpret_cast<const int*>(sg);
+      for (int e = tid; e < 2 * gim; e += kBlock)
+        sg[e] = (R)(fmaf((float)gi[e], 65536.0f, (float)gi[e + 2 * gim]) * inv);
+      __syncthreads();
+    }
     MLIPG_STAMP(4)
     // ---------------------------------------------------------------- P6
     double fix = 0.0, fiy = 0.0, fiz = 0.0;

@@ -15,6 +15,7 @@ constexpr int kLhMax = (kMaxL + 1) * (kMaxL + 2) / 2;
 enum StatusBits : int {
   kStatusNeighbourCapacity = 1,  // an atom had more neighbours inside rc than nb_cap
   kStatusBadType = 2,            // an element index outside [0, T) in the inputs
+  kStatusAdjointRange = 4,       // mixed path: adjoint flushes out of the fixed-point range
 };
 
 struct KernelArgs {
@@ -47,6 +48,7 @@ struct KernelArgs {
   const double* radial;   // [F][2] (beta, mu)
   int T, F, L, Lh, nb_cap, nl_cap;
   double rc;
+  float g_bound;          // mixed path: largest fixed-point adjoint flush (power of two)
   // outputs
   double* f;              // [nforce][3], accumulated with atomics
   double* eatom;          // [ncenters] (may be null)

@@ -324,6 +324,34 @@ std::vector<U> deal_longest_first(std::vector<U> v, Cost cost, double* load, con
   return out;
 }
 
+// Upper bound of the adjoint flushes one order-parameter row lm of a centre
+// of element t receives: every term of every unit flushes each slot at most
+// once (counted per lm over all elements of the slot, which over-counts).
+int max_flushes_per_entry(const Model& M, int t) {
+  const Schedule& S = M.sched[t];
+  std::vector<int> cnt(std::max(M.Lh, 1), 0);
+  const auto add_terms = [&](int term0, int nterm, int q) {
+    for (int k = term0; k < term0 + nterm; ++k)
+      for (int p = 0; p < q; ++p) cnt[M.cterms[k].lmh[p]]++;
+  };
+  for (const DeviceIrrUnit& u : S.iunits)
+    if (u.nterm > 0) add_terms(u.term0, u.nterm, u.q);
+  for (const DeviceUnit& u : S.units)
+    if (u.nterm > 0) add_terms(u.term0, u.nterm, u.q);
+  return *std::max_element(cnt.begin(), cnt.end());
+}
+
+void set_adjoint_bound(Model& M) {
+  int cmax = 1;
+  for (int t = 0; t < M.T; ++t) cmax = std::max(cmax, max_flushes_per_entry(M, t));
+  // high parts are multiples of 2^16 (at most bound / 2^16 each): their int32
+  // sum stays below 2^31; the high-part rounding is exact below 2^38; low
+  // parts (|.| <= 2^15) cannot overflow for fewer than 2^16 flushes
+  double b = 274877906944.0;   // 2^38
+  while ((b / 65536.0) * (cmax + 1) >= 2147483648.0 && b > 65536.0) b *= 0.5;
+  M.g_bound = cmax < 65535 ? b : 0.0;   // 0: no fixed-point accumulation possible
+}
+
 bool schedules_for_tiling(Model& M, std::string& err) {
   const int T = M.T, F = M.F;
   // nonlinear itc: appear in any polynomial term of order >= 2
@@ -498,7 +526,9 @@ bool build_schedules(Model& M, std::string& err) {
     err = "invalid tiling";
     return false;
   }
-  return schedules_for_tiling(M, err);
+  if (!schedules_for_tiling(M, err)) return false;
+  set_adjoint_bound(M);
+  return true;
 }
 
 bool read_potential(const std::string& path, Potential& p, std::string& err) {
@@ -656,7 +686,9 @@ bool build_model(Model& M, std::string& err) {
     M.other_type[tc * M.T + tpm[tc].second] = tpm[tc].first;
   }
   if (!fold_terms(M, err)) return false;
-  return schedules_for_tiling(M, err);
+  if (!schedules_for_tiling(M, err)) return false;
+  set_adjoint_bound(M);
+  return true;
 }
 
 bool count_coefficients(int n_types, int model_type, int maxp, int maxl, int gtinv_order,

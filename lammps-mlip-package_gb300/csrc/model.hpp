@@ -137,6 +137,10 @@ struct Model {
   std::vector<Schedule> sched;                // [T]
   Tiling tiling;
   int max_nl = 0;                             // max nonlinear itc over elements
+  // Largest scaled adjoint flush allowed in the mixed path's fixed-point
+  // adjoint accumulation (high parts in multiples of 2^16): a power of two with
+  // (flushes per entry) x bound / 2^16 < 2^31, so no integer sum overflows.
+  double g_bound = 274877906944.0;
 };
 
 // Parses a potential file; returns false with `err` set on failure.
