@@ -293,14 +293,13 @@ __device__ __forceinline__ void pair_disp(const KernelArgs& A, int c, int k, con
 // Each flush is scaled by 2^e (e adapted per centre element) and split
 // exactly into a high part, a multiple of 2^16, and a low part of at most
 // 2^15 (both rounded by the exact magic-number add), which go to two int32
-// arrays (low part at p + lo_off); no carries are needed because the host
+// arrays (the low-part array follows the high parts of re and im); no carries are needed because the host
 // bounds the flushes per entry.  Sums are exact and order independent; the
 // centre's largest |scaled flush| is tracked so that out-of-range flushes are
 // detected (the invariant phase is then redone at a smaller scale).
 struct GFix {
   R scale;     // 2^e
   R vmax;      // largest |scaled flush| of this thread
-  int lo_off;  // element offset of the low-part array (2 x the imaginary offset)
 };
 // y: the flush already multiplied by g.scale (1 in FP64); lo: element offset
 // of the low-part array (2 x the imaginary offset)
@@ -382,8 +381,8 @@ __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* 
         // flush free of divergent branches
         R* gp = sg + off[p] + lmh[p] * kNPad;
         const R cs = cc * gf.scale;
-        gput(gp, cs * kr * Pr, gf, gf.lo_off);
-        gput(gp + gim, cs * ki * Pi, gf, gf.lo_off);
+        gput(gp, cs * kr * Pr, gf, 2 * gim);
+        gput(gp + gim, cs * ki * Pi, gf, 2 * gim);
       }
     }
   }
@@ -1021,7 +1020,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       for (int u = warp; u < nNL; u += kBlock / 32) {
         const DeviceUnit un = A.nl_units[nl0 + u];
         R dsum = R(0);
-        GFix gnone{R(1), R(0), 0};
+        GFix gnone{R(1), R(0)};
         dispatch_unit<false, LS>(un, A.terms, sa, sg, gim, gnone, n, half, act, R(0), dsum);
         dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
         if (half == 0) dnl[u * kNPad + n] = act ? (double)dsum : 0.0;
@@ -1072,7 +1071,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     gexp = misc[16 + ti];
     if (tid == 0) misc[12] = 0;
     __syncthreads();   // G zeroed; everyone has read this attempt's scale
-    GFix gf{sizeof(R) == 4 ? (R)ldexpf(1.0f, gexp) : R(1), R(0), 2 * gim};
+    GFix gf{sizeof(R) == 4 ? (R)ldexpf(1.0f, gexp) : R(1), R(0)};
     {
       const int u0 = __ldg(A.unit_off + ti), nU = __ldg(A.unit_off + ti + 1) - u0;
       const int i0 = __ldg(A.iunit_off + ti), nI = __ldg(A.iunit_off + ti + 1) - i0;
