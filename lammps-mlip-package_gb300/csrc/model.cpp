@@ -511,7 +511,19 @@ bool schedules_for_tiling(Model& M, std::string& err) {
       DeviceUnit upad{};
       upad.itc = -1;
       upad.nl_slot = -1;
-      S.iunits = deal_longest_first(S.iunits, icost, load, ipad);
+      // dealt one order at a time (highest first), so that the warps run the
+      // same unit variant at the same time (one code path in the
+      // instruction cache); balance carries over between the groups
+      std::vector<DeviceIrrUnit> dealt;
+      for (int q = kMaxOrder; q >= 1; --q) {
+        std::vector<DeviceIrrUnit> grp;
+        for (const DeviceIrrUnit& u : S.iunits)
+          if (u.q == q) grp.push_back(u);
+        if (grp.empty()) continue;
+        grp = deal_longest_first(grp, icost, load, ipad);
+        dealt.insert(dealt.end(), grp.begin(), grp.end());
+      }
+      S.iunits = dealt;
       S.units = deal_longest_first(S.units, ucost, load, upad);
     }
   }
