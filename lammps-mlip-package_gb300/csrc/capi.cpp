@@ -83,6 +83,7 @@ struct mlipg_handle {
   cudaStream_t stream = nullptr;
   // model tables on the device
   DevBuf d_terms, d_units, d_unit_off, d_nl, d_nl_off, d_poly, d_poly_off, d_wlin, d_radial;
+  DevBuf d_terms_f;   // the same terms with the coefficient as FP32 (mixed path)
   DevBuf d_iunits, d_iunit_off, d_tuples, d_wlin_f, d_phase, d_adj_base, d_adj_off, d_adj;
   // per-call buffers (grow only)
   DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_vatom, d_partials, d_status, d_out8;
@@ -162,6 +163,15 @@ static int upload_model(mlipg_handle* h) {
   }
   cudaStream_t s = h->stream;
   CK(upload(h->d_terms, M.cterms, s), "upload terms");
+  {
+    std::vector<DeviceTerm> tf(M.cterms);
+    for (DeviceTerm& t : tf) {
+      const float cf = (float)t.c;
+      t.c = 0.0;
+      std::memcpy(&t.c, &cf, sizeof cf);   // low word of the 8-byte field
+    }
+    CK(upload(h->d_terms_f, tf, s), "upload FP32 terms");
+  }
   CK(upload(h->d_units, units, s), "upload units");
   CK(upload(h->d_iunits, iunits, s), "upload batched units");
   CK(upload(h->d_iunit_off, ioff, s), "upload batched unit offsets");
@@ -249,7 +259,8 @@ int mlipg_destroy(mlipg_handle* h) {
   }
   DevBuf* bufs[] = {&h->d_adj_base, &h->d_adj_off, &h->d_adj,
                     &h->d_iunits, &h->d_iunit_off, &h->d_tuples, &h->d_wlin_f, &h->d_phase,
-                    &h->d_terms, &h->d_units, &h->d_unit_off, &h->d_nl, &h->d_nl_off,
+                    &h->d_terms, &h->d_terms_f, &h->d_units, &h->d_unit_off, &h->d_nl,
+                    &h->d_nl_off,
                     &h->d_poly, &h->d_poly_off, &h->d_wlin, &h->d_radial, &h->d_x4,
                     &h->d_centers, &h->d_off, &h->d_idx, &h->d_f, &h->d_eatom, &h->d_vatom, &h->d_partials,
                     &h->d_status, &h->d_out8};
@@ -351,7 +362,7 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.center_cell = center_cell;
   a.fold = fold;
   a.ncenters = ncenters;
-  a.terms = h->d_terms.as<DeviceTerm>();
+  a.terms = (fp64 ? h->d_terms : h->d_terms_f).as<DeviceTerm>();
   a.units = h->d_units.as<DeviceUnit>();
   a.unit_off = h->d_unit_off.as<int>();
   a.iunits = h->d_iunits.as<DeviceIrrUnit>();
@@ -798,7 +809,7 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
   a.center_cell = d_center_cell;
   a.fold = d_fold;
   a.ncenters = ncenters;
-  a.terms = h->d_terms.as<DeviceTerm>();
+  a.terms = (fp64 ? h->d_terms : h->d_terms_f).as<DeviceTerm>();
   a.units = h->d_units.as<DeviceUnit>();
   a.unit_off = h->d_unit_off.as<int>();
   a.iunits = h->d_iunits.as<DeviceIrrUnit>();

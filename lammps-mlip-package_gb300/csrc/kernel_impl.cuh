@@ -287,6 +287,13 @@ __device__ __forceinline__ void pair_disp(const KernelArgs& A, int c, int k, con
 }
 
 // One coupling unit for all n: warp halves take alternate terms.
+// Coupling coefficient of a term record: FP64 in the FP64 path's table; the
+// mixed path's table holds it as FP32 in the low word (no conversion per term).
+__device__ __forceinline__ R term_coeff(const int4& raw) {
+  if constexpr (sizeof(R) == 4) return __int_as_float(raw.x);
+  else return __hiloint2double(raw.y, raw.x);
+}
+
 // Adjoint accumulation into shared memory.  FP64: double atomics.  Mixed
 // path: exact 64-bit fixed point with native 32-bit integer atomics (a
 // shared-memory FP32 atomic add is a compare-and-swap loop, six times slower).
@@ -325,7 +332,7 @@ __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* 
   const int kend = u.term0 + u.nterm;
   for (int k = u.term0 + half; k < kend; k += 2) {
     const int4 raw = __ldg(reinterpret_cast<const int4*>(terms + k));
-    const R c = (R)__hiloint2double(raw.y, raw.x);
+    const R c = term_coeff(raw);
     const unsigned lw = (unsigned)raw.z, hw = (unsigned)raw.w;
     const unsigned code = hw >> 16;
     int lmh[Q];
@@ -431,7 +438,7 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
   const int kend = u.term0 + u.nterm;
   for (int k = u.term0 + half; k < kend; k += 2) {
     const int4 raw = __ldg(reinterpret_cast<const int4*>(terms + k));
-    const R c = (R)__hiloint2double(raw.y, raw.x);
+    const R c = term_coeff(raw);
     const unsigned lw = (unsigned)raw.z, code = ((unsigned)raw.w) >> 16;
     const bool self = (code >> 12) & 1u;
     const R ce = self ? c : R(2) * c;
@@ -619,7 +626,7 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
     const int4 raw = nxt;
     if (k + 2 < ke) nxt = __ldg(reinterpret_cast<const int4*>(terms + k + 2));
     const bool last = k + 2 >= ke;
-    const R c = (R)__hiloint2double(raw.y, raw.x);
+    const R c = term_coeff(raw);
     const unsigned lw = (unsigned)raw.z, code = ((unsigned)raw.w) >> 16;
     const bool self = (code >> 12) & 1u;
     const R ce = self ? c : R(2) * c;
