@@ -223,12 +223,15 @@ void mlipg_dnlist_destroy(mlipg_dnlist* L);
  * reference (its Kokkos team sizes are fixed at compile time).
  * irr_chunk: coupling terms per batched work unit (even, 2..4096; default 24);
  * warp_order: 0 = units dealt round robin to the CTA's 8 warps in cost order,
- *             1 = longest first onto the least-loaded warp;
+ *             1 = longest first onto the least-loaded warp (one coupling order
+ *                 at a time),
+ *             2 = taken by the warps from a shared counter (order by order,
+ *                 longest first);
  * ctas_per_sm: CTAs per SM of the persistent grid (0 = as many as fit).
  * Results agree between tilings to rounding (the energy summation is grouped
  * by unit).  mlipg_set_tiling waits for the handle's stream and re-uploads the
  * schedules; MD objects re-capture their step graph afterwards.
- * mlipg_autotune times every candidate (irr_chunk 12/24/48 x both orders x
+ * mlipg_autotune times every candidate (irr_chunk 12/24/48 x the three orders x
  * 1..resident CTAs/SM) on up to 16 centres per resident CTA of the given
  * structure (same arguments as mlipg_compute_device), keeps the fastest and
  * writes rows [irr_chunk, warp_order, ctas_per_sm, ms] to report (up to

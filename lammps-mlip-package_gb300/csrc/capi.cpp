@@ -387,6 +387,7 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.nl_cap = nl_cap;
   a.rc = M.pot.cutoff;
   a.g_bound = (float)M.g_bound;
+  a.unit_dyn = M.tiling.warp_order == 2 ? 1 : 0;
   a.f = f;
   a.eatom = eatom;
   a.vatom = vatom;
@@ -724,7 +725,7 @@ extern "C" int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4,
   CK(cudaEventCreate(&e1), "event create");
   int rc = MLIPG_OK;
   for (int chunk : {12, 24, 48})
-    for (int order : {0, 1})
+    for (int order : {0, 1, 2})
       for (int cps = 1; cps <= bps_max && rc == MLIPG_OK; ++cps) {
         rc = mlipg_set_tiling(h, chunk, order, cps);
         if (rc != MLIPG_OK) break;
@@ -834,6 +835,7 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
   a.nl_cap = nl_cap;
   a.rc = M.pot.cutoff;
   a.g_bound = (float)M.g_bound;
+  a.unit_dyn = M.tiling.warp_order == 2 ? 1 : 0;
   a.f = d_f;
   a.eatom = d_eatom;
   a.vatom = d_vatom;

@@ -294,6 +294,13 @@ __device__ __forceinline__ R term_coeff(const int4& raw) {
   else return __hiloint2double(raw.y, raw.x);
 }
 
+// Sum of the batched units' energies taken from a shared counter: the two
+// 64-bit integer parts (2^-20 eV and 2^-60 eV) kept at misc[24..27].
+__device__ __forceinline__ double unit_energy(const int* misc) {
+  const unsigned long long* e = reinterpret_cast<const unsigned long long*>(misc + 24);
+  return (double)(long long)e[0] * 0x1p-20 + (double)(long long)e[1] * 0x1p-60;
+}
+
 // Adjoint accumulation into shared memory.  FP64: double atomics.  Mixed
 // path: exact 64-bit fixed point with native 32-bit integer atomics (a
 // shared-memory FP32 atomic add is a compare-and-swap loop, six times slower).
@@ -1076,7 +1083,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     for (int attempt = 0;; ++attempt) {
     for (int e = tid; e < (sizeof(R) == 4 ? 4 : 2) * gim; e += kBlock) sg[e] = R(0);
     gexp = misc[16 + ti];
-    if (tid == 0) misc[12] = 0;
+    if (tid == 0) {
+      misc[12] = 0;
+      misc[13] = 0;   // unit counter
+      reinterpret_cast<unsigned long long*>(misc + 24)[0] = 0ull;   // unit energies
+      reinterpret_cast<unsigned long long*>(misc + 24)[1] = 0ull;
+    }
     __syncthreads();   // G zeroed; everyone has read this attempt's scale
     GFix gf{sizeof(R) == 4 ? (R)ldexpf(1.0f, gexp) : R(1), R(0)};
     {
@@ -1085,15 +1097,41 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       // static round-robin over warps (units are sorted by cost): each
       // thread's energy sum has a fixed order, so energies are reproducible
       const R* wl = wlin_table(A);
-      for (int u = warp; u < nI; u += kBlock / 32) {
-        const DeviceIrrUnit iu = A.iunits[i0 + u];
-        if (iu.nterm == 0) continue;   // padding of a balanced schedule
+      const auto run_iu = [&](const DeviceIrrUnit& iu, double& e) {
         if (T == 3)
-          dispatch_irr<3, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, eacc);
+          dispatch_irr<3, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, e);
         else if (T == 2)
-          dispatch_irr<2, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, eacc);
+          dispatch_irr<2, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, e);
         else
-          dispatch_irr<1, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, eacc);
+          dispatch_irr<1, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, e);
+      };
+      if (A.unit_dyn) {
+        // warps take units from a shared counter (no end-of-phase imbalance);
+        // each unit's energy is split exactly into 2^-20 eV and 2^-60 eV
+        // integer parts and added to two 64-bit sums, so the total does not
+        // depend on which warp ran which unit
+        unsigned long long* efix = reinterpret_cast<unsigned long long*>(misc + 24);
+        for (;;) {
+          int u = 0;
+          if (lane == 0) u = atomicAdd(misc + 13, 1);
+          u = __shfl_sync(0xffffffffu, u, 0);
+          if (u >= nI) break;
+          double e = 0.0;
+          run_iu(A.iunits[i0 + u], e);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+          if (lane == 0) {
+            const double sc = e * 0x1p20, hi = rint(sc);
+            atomicAdd(efix, (unsigned long long)(long long)hi);
+            atomicAdd(efix + 1, (unsigned long long)__double2ll_rn((sc - hi) * 0x1p40));
+          }
+        }
+      } else {
+        for (int u = warp; u < nI; u += kBlock / 32) {
+          const DeviceIrrUnit iu = A.iunits[i0 + u];
+          if (iu.nterm == 0) continue;   // padding of a balanced schedule
+          run_iu(iu, eacc);
+        }
       }
       MLIPG_STAMP(3)   // warp 0's batched units (the warps' shares are balanced)
       for (int u = warp; u < nU; u += kBlock / 32) {
@@ -1112,6 +1150,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     }
     if (sizeof(R) != 4) {
       __syncthreads();
+      if (A.unit_dyn && tid == 0)
+        eacc += unit_energy(misc);
       break;
     }
     {
@@ -1134,6 +1174,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     }
     if ((!out && !coarse) || attempt >= 2) {
       if (out && tid == 0) atomicOr(A.status, kStatusAdjointRange);
+      if (A.unit_dyn && tid == 0)
+        eacc += unit_energy(misc);
       break;
     }
     eacc = eacc0;

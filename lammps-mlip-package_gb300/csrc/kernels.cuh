@@ -49,6 +49,7 @@ struct KernelArgs {
   int T, F, L, Lh, nb_cap, nl_cap;
   double rc;
   float g_bound;          // mixed path: largest fixed-point adjoint flush (power of two)
+  int unit_dyn;           // 1: warps take batched units from a shared counter
   // outputs
   double* f;              // [nforce][3], accumulated with atomics
   double* eatom;          // [ncenters] (may be null)

@@ -496,6 +496,15 @@ bool schedules_for_tiling(Model& M, std::string& err) {
         err = "internal error: work schedule does not cover every feature once";
         return false;
       }
+    if (M.tiling.warp_order == 2) {
+      // taken by the warps from a shared counter in this order: one coupling
+      // order at a time (same code path), longest units first
+      std::stable_sort(S.iunits.begin(), S.iunits.end(),
+                       [](const DeviceIrrUnit& a, const DeviceIrrUnit& b) {
+                         if (a.q != b.q) return a.q > b.q;
+                         return a.nterm > b.nterm;
+                       });
+    }
     if (M.tiling.warp_order == 1) {
       // per-warp cost ~ terms x tuples x order (products and adjoint products)
       // batched unit per term: products over the tuple block, one atomic
@@ -534,7 +543,7 @@ bool schedules_for_tiling(Model& M, std::string& err) {
 
 bool build_schedules(Model& M, std::string& err) {
   if (M.tiling.irr_chunk < 2 || M.tiling.irr_chunk > 4096 || M.tiling.irr_chunk % 2 ||
-      M.tiling.warp_order < 0 || M.tiling.warp_order > 1 || M.tiling.ctas_per_sm < 0) {
+      M.tiling.warp_order < 0 || M.tiling.warp_order > 2 || M.tiling.ctas_per_sm < 0) {
     err = "invalid tiling";
     return false;
   }

@@ -92,7 +92,8 @@ constexpr int kCtaWarps = 8;   // warps of the fused kernel's CTA (units are dea
 // Tile shape of the fused kernel's invariant/adjoint phase, chosen by the
 // autotuner: terms per batched unit, the order in which units are dealt to
 // the CTA's warps (0 = cost-sorted round robin, 1 = longest-first onto the
-// least-loaded warp, padded with empty units), and CTAs per SM of the
+// least-loaded warp, padded with empty units, 2 = taken dynamically from a
+// shared counter), and CTAs per SM of the
 // persistent grid (0 = as many as are resident).
 struct Tiling {
   int irr_chunk = kIrrChunk;

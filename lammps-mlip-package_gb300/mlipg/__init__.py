@@ -177,6 +177,8 @@ class Potential:
             "n_coeffs", "model_type", "maxp", "max_nonlinear_itc"]
 
     def __init__(self, path: str, precision: int = PREC_FP64):
+        import weakref
+        self._children = weakref.WeakSet()   # batches / MD runs built on this handle
         h = ctypes.c_void_p()
         _check(lib().mlipg_create(os.fsencode(path), precision, ctypes.byref(h)))
         self.h = h
@@ -190,6 +192,10 @@ class Potential:
         self.cutoff = lib().mlipg_cutoff(self.h)
 
     def close(self):
+        # objects that use this handle's stream go first (in a garbage-collected
+        # cycle the handle may be finalized before them)
+        for child in list(getattr(self, "_children", ())):
+            child.close()
         if getattr(self, "h", None):
             lib().mlipg_destroy(self.h)
             self.h = None
@@ -338,6 +344,7 @@ class MD:
         if rc != 0:
             raise MlipgError(rc, lib().mlipg_last_error(potential.h).decode())
         self.h = h
+        potential._children.add(self)
 
     def run(self, nsteps: int, dt: float = 0.001, graph: bool = True):
         rc = lib().mlipg_md_run(self.h, nsteps, dt, 1 if graph else 0)
@@ -408,6 +415,7 @@ class Batch:
         if rc != 0:
             raise MlipgError(rc, "mlipg_batch_create failed")
         self.h = h
+        potential._children.add(self)
         na = ctypes.c_int()
         npairs = ctypes.c_longlong()
         lib().mlipg_batch_sizes(self.h, ctypes.byref(na), ctypes.byref(npairs))

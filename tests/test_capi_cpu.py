@@ -102,10 +102,10 @@ def test_tiling_candidates_build_on_host(tmp_path):
         workload_potential(p, name)
         g = mlipg.Potential(p, mlipg.PREC_MIXED)
         for chunk in (12, 24, 48):
-            for order in (0, 1):
+            for order in (0, 1, 2):
                 g.set_tiling(chunk, order, 1)
                 assert g.tiling() == {"irr_chunk": chunk, "warp_order": order, "ctas_per_sm": 1}
-        for bad in ((13, 0, 0), (24, 2, 0), (24, 0, -1), (0, 0, 0)):
+        for bad in ((13, 0, 0), (24, 3, 0), (24, 0, -1), (0, 0, 0)):
             with pytest.raises(mlipg.MlipgError):
                 g.set_tiling(*bad)
         assert g.tiling()["irr_chunk"] == 48

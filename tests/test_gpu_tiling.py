@@ -18,7 +18,7 @@ from oracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
-TILINGS = [(12, 0, 0), (12, 1, 1), (24, 1, 0), (48, 0, 1), (48, 1, 0)]
+TILINGS = [(12, 0, 0), (12, 1, 1), (24, 1, 0), (48, 0, 1), (48, 1, 0), (24, 2, 0), (48, 2, 1)]
 
 
 def rel(a, b):
