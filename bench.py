@@ -394,9 +394,16 @@ def run_ours(args, dist):
            "d2h_bytes_per_step": int(24 * sysm.nall + 8 * 8 + 4),
            "api": "mlipg_compute (LAMMPS-shaped host arrays)"}
 
-    # ---------------- plain FP64 path on a bounded subset of centres
+    # ---------------- plain FP64 path on a bounded subset of centres, with
+    # its own tile shape (autotuned for FP64 unless one is fixed)
+    mixed_tiling = g.tiling()
     g.set_precision(mlipg.PREC_FP64)
     nsub = max(1024, min(natoms, int(natoms * args.fp64_fraction)))
+    fp64_tiling = None
+    if args.autotune:
+        g.autotune_device(min(nsub, 9728), d_x4.data_ptr(), d_cent.data_ptr(), d_off.data_ptr(),
+                          d_idx.data_ptr(), d_f.data_ptr(), d_out.data_ptr(), nb_cap=nb_cap)
+        fp64_tiling = g.tiling()
     step(nsub)
     torch.cuda.synchronize()
     ev0.record(stream)
@@ -406,6 +413,8 @@ def run_ours(args, dist):
     torch.cuda.synchronize()
     fp64_v = nsub * 2 / (ev0.elapsed_time(ev1) * 1e-3)
     g.set_precision(mlipg.PREC_MIXED)
+    g.set_tiling(mixed_tiling["irr_chunk"], mixed_tiling["warp_order"],
+                 mixed_tiling["ctas_per_sm"])
 
     # ---------------- accuracy of mixed vs FP64 on a 4,000-atom cell
     small = mlipg.native_system(make_cell(spec, n=10 if spec["lattice"] == "fcc" else 13,
@@ -459,7 +468,7 @@ def run_ours(args, dist):
                            "step": "energy + forces + virial of all atoms, one fused launch",
                            "tiling": tune},
                 "e2e": e2e,
-                "fp64": {"value": fp64_v, "unit": UNIT, "centres": nsub,
+                "fp64": {"value": fp64_v, "unit": UNIT, "centres": nsub, "tiling": fp64_tiling,
                          "mixed_over_fp64": value / dist["world"] / fp64_v},
                 "accuracy_mixed_vs_fp64": acc,
                 "energy_eV": e_mixed,
