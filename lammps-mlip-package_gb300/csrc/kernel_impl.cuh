@@ -5,7 +5,8 @@
 // shared memory:
 //   P1  neighbour compaction: keep r <= rc, stable-sort by element (warp 0)
 //   P2  order parameters a[s][lm][n] = sum_j f_n(r) conj(Y_lm): f_n and Y_lm
-//       evaluated in REAL, staged as FP64 and summed with FP64 FMAs
+//       evaluated in REAL; FP64 path: staged as FP64 and summed with FP64
+//       FMAs; mixed path: FP32 products summed with TwoSum compensation
 //       (mlipkk_lmp.h:314-387, mlipkk_features_kk.h:9-48,
 //       mlipkk_spherical_harmonics_kk.h:18-81)
 //   P3  nonlinear features and polynomial terms of order >= 2: energy part
@@ -187,8 +188,6 @@ __device__ __forceinline__ void radial(const double* __restrict__ prm, int F, R 
   }
 }
 
-// Stages Y_lm of one neighbour as FP64 (exact conversion of the REAL value)
-// for the FP64 order-parameter sums.
 // radial basis for the 4 channels n0..n0+3 (P6: 4 threads per neighbour)
 __device__ __forceinline__ void radial4(const double* __restrict__ prm, int F, int n0, R r, R rc,
                                         R* f, R* fd) {
@@ -213,6 +212,8 @@ __device__ __forceinline__ void radial4(const double* __restrict__ prm, int F, i
   }
 }
 
+// Stages Y_lm of one neighbour as FP64 (exact conversion of the REAL value)
+// for the FP64 order-parameter sums.
 struct StageVis {
   double2* ys;
   int slot;
@@ -220,6 +221,27 @@ struct StageVis {
     ys[lmh * kChunk + slot] = double2{(double)yre, (double)yim};
   }
 };
+
+// Stages Y_lm of one neighbour as FP32 pairs for the mixed path's
+// compensated FP32 order-parameter sums.
+struct StageVisF {
+  float2* ys;
+  int slot;
+  __device__ __forceinline__ void operator()(int lmh, int, R yre, R yim, R, R, R, R, R, R) {
+    ys[lmh * kChunk + slot] = float2{(float)yre, (float)yim};
+  }
+};
+
+// s + c += p with Knuth's TwoSum: s keeps the rounded running sum, c gathers
+// every addition's exact rounding error (explicit _rn intrinsics, so nothing
+// is contracted or reassociated).
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float p) {
+  const float t = __fadd_rn(s, p);
+  const float bp = __fsub_rn(t, s);
+  const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  c = __fadd_rn(c, e);
+  s = t;
+}
 
 // four consecutive values from 16-byte aligned shared memory
 __device__ __forceinline__ void load4(const float* p, float* v) {
@@ -980,6 +1002,60 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     const int nkeep = misc[T];
     MLIPG_STAMP(0)
     // ---------------------------------------------------------------- P2
+    if constexpr (sizeof(R) == 4 && LCAP <= 16) {
+      // Mixed path: FP32 products summed with TwoSum compensation (sum and
+      // error term per entry), rounded once to FP32 at the end; the FP32
+      // pipe is some sixty times wider than the FP64 pipe on this GPU.  (At
+      // l <= 20 the four accumulators per entry no longer fit in registers
+      // beside the rest, so that instantiation keeps the FP64 sums.)
+      float2* ysf = reinterpret_cast<float2*>(sg);
+      float* fsf = reinterpret_cast<float*>(smem + lay.g + (size_t)LS * kChunk * sizeof(float2));
+      const int n = tid & 15;
+      for (int t = 0; t < T; ++t) {
+        float sr[kEPT], cr[kEPT], si[kEPT], ci[kEPT];
+#pragma unroll
+        for (int e = 0; e < kEPT; ++e) { sr[e] = 0.f; cr[e] = 0.f; si[e] = 0.f; ci[e] = 0.f; }
+        const int b0 = misc[t], b1 = misc[t + 1];
+        for (int cb = b0; cb < b1; cb += kChunk) {
+          const int csz = min(kChunk, b1 - cb);
+          if (tid < csz) {
+            const int k = nbk[cb + tid];
+            const int j = __ldg(A.nbr_idx + k);
+            double dx, dy, dz;
+            pair_disp(A, c, k, xi, A.x4[j], dx, dy, dz);
+            const double r = sqrt(dx * dx + dy * dy + dz * dz);
+            R f[kNPad], fdum[kNPad];
+            radial(A.radial, F, (R)r, rc, f, fdum, false);
+#pragma unroll
+            for (int q = 0; q < kNPad; ++q) fsf[tid * kNPad + q] = (float)f[q];
+            StageVisF v{ysf, tid};
+            sh_visit<LCAP, false>((R)dx, (R)dy, (R)dz, (R)r, L, v);
+          }
+          __syncthreads();
+#pragma unroll
+          for (int e = 0; e < kEPT; ++e) {
+            // rows past Lh read a staged row and are never stored
+            const float2* yrow = ysf + min((tid + e * kBlock) >> 4, Lh - 1) * kChunk;
+#pragma unroll 4
+            for (int jj = 0; jj < csz; ++jj) {
+              const float fv = fsf[jj * kNPad + n];
+              const float2 y = yrow[jj];
+              two_sum_acc(sr[e], cr[e], __fmul_rn(fv, y.x));
+              two_sum_acc(si[e], ci[e], __fmul_rn(-fv, y.y));
+            }
+          }
+          __syncthreads();
+        }
+#pragma unroll
+        for (int e = 0; e < kEPT; ++e) {
+          const int idx = tid + e * kBlock;
+          const int lmh = idx >> 4;
+          if (lmh < Lh)
+            sa[(t * LS + lmh) * kNPad + (idx & 15)] =
+                Rc{(R)__fadd_rn(sr[e], cr[e]), (R)__fadd_rn(si[e], ci[e])};
+        }
+      }
+    } else
     for (int t = 0; t < T; ++t) {
       double accr[kEPT], acci[kEPT];
 #pragma unroll
