@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "kernels.cuh"
 
@@ -243,6 +244,39 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float p) {
   s = t;
 }
 
+// Per-thread energy sum of the batched units.  FP64 path: a double.  Mixed
+// path: a TwoSum pair in FP32 (running sum, gathered rounding errors), folded
+// into the centre's FP64 energy once per centre.
+struct ESumF {
+  float s = 0.f, c = 0.f;
+};
+__device__ __forceinline__ void eadd(double& e, double v) { e += v; }
+__device__ __forceinline__ void eadd(ESumF& e, float v) { two_sum_acc(e.s, e.c, v); }
+
+// Sum over the warp's lanes of one unit's energy, identical on every lane.
+// FP64: a butterfly of FP64 adds.  Mixed: a butterfly of TwoSum steps in FP32
+// (each step's rounding error is exact and the pair's sum is commutative, so
+// partners agree bit for bit), returned as the FP64 value of sum + error.
+__device__ __forceinline__ double warp_energy(double e) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+  return e;
+}
+__device__ __forceinline__ double warp_energy(ESumF e) {
+  float s = e.s, c = e.c;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float so = __shfl_xor_sync(0xffffffffu, s, o);
+    const float co = __shfl_xor_sync(0xffffffffu, c, o);
+    const float t = __fadd_rn(s, so);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(so, bp));
+    c = __fadd_rn(__fadd_rn(c, co), err);
+    s = t;
+  }
+  return (double)s + (double)c;
+}
+
 // four consecutive values from 16-byte aligned shared memory
 __device__ __forceinline__ void load4(const float* p, float* v) {
   const float4 t = *reinterpret_cast<const float4*>(p);
@@ -438,12 +472,12 @@ __device__ __forceinline__ const R* wlin_table(const KernelArgs& A) {
 // slot's partials (sum_j H_j Pi_j = sum_s g_last[s] a_last[s]).  Shorter
 // dependency chains than the factorized form, which pays off only with
 // three elements.
-template <int Q, int TT, int Lh>
+template <int Q, int TT, int Lh, class EA>
 __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
-                                        const R* __restrict__ wlin, const double* hnl,
+                                        const R* __restrict__ wlin, const R* hnl,
                                         const Rc* sa, R* sg, int gim, GFix& gf, int n,
-                                        int half, bool act, double& eacc) {
+                                        int half, bool act, EA& eacc) {
   constexpr int N0 = TT;                                  // elements of slot 0
   constexpr int NT = (Q == 1) ? N0 : (Q == 2 ? N0 * TT : N0 * TT * TT);
   constexpr int s0base = 0;
@@ -454,7 +488,7 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
     R h = R(0);
     if (act && e.x >= 0) {
       h = __ldg(wlin + (size_t)e.x * kNPad + n);
-      if (e.y >= 0) h = (R)((double)h + hnl[e.y * kNPad + n]);
+      if (e.y >= 0) h += hnl[e.y * kNPad + n];
     }
     H[j] = h;
   }
@@ -584,9 +618,9 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
       }
     }
   }
-  // this half-warp's terms, in REAL, into the centre's FP64 energy (zero on
+  // this half-warp's terms, in REAL, into the thread's energy sum (zero on
   // lanes n >= F)
-  eacc += (double)eu;
+  eadd(eacc, eu);
 }
 
 // acc += a * b (complex) as two fused multiply-add chains
@@ -610,12 +644,12 @@ __device__ __forceinline__ void cmac(R& accr, R& acci, R ar, R ai, R br, R bi) {
 // order-parameter loads per term; the adjoint partials of x and y are summed
 // over z in registers and flushed with one shared-memory atomic per (slot,
 // element).
-template <int Q, int TT, int Lh>
+template <int Q, int TT, int Lh, class EA>
 __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
-                                        const R* __restrict__ wlin, const double* hnl,
+                                        const R* __restrict__ wlin, const R* hnl,
                                         const Rc* sa, R* sg, int gim, GFix& gf, int n,
-                                        int half, bool act, double& eacc) {
+                                        int half, bool act, EA& eacc) {
   constexpr int NZ = (Q >= 3) ? TT : 1;      // elements of slot z
   constexpr int NX = TT;                     // elements of slot x (slot 0 for Q = 1)
   constexpr int NY = (Q == 1) ? 1 : TT;      // elements of slot y
@@ -634,7 +668,7 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
         R h = R(0);
         if (act && e.x >= 0) {
           h = __ldg(wlin + (size_t)e.x * kNPad + n);
-          if (e.y >= 0) h = (R)((double)h + hnl[e.y * kNPad + n]);
+          if (e.y >= 0) h += hnl[e.y * kNPad + n];
         }
         H[z][x][y] = h;
       }
@@ -811,16 +845,16 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       }
     }
   }
-  // this half-warp's terms, in REAL, into the centre's FP64 energy (zero on
+  // this half-warp's terms, in REAL, into the thread's energy sum (zero on
   // lanes n >= F)
-  eacc += (double)eu;
+  eadd(eacc, eu);
 }
 
-template <int TT, int Lh>
+template <int TT, int Lh, class EA>
 __device__ __forceinline__ void dispatch_irr(const DeviceIrrUnit& u, const DeviceTuple* tups,
                                              const DeviceTerm* terms, const R* wlin,
-                                             const double* hnl, const Rc* sa, R* sg, int gim,
-                                             GFix& gf, int n, int half, bool act, double& eacc) {
+                                             const R* hnl, const Rc* sa, R* sg, int gim,
+                                             GFix& gf, int n, int half, bool act, EA& eacc) {
   if (TT <= 2 && u.q <= 3) {
     switch (u.q) {
       case 1: run_irr_direct<1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
@@ -1150,6 +1184,15 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     // P5 weighs every feature's products with H = w + dE_poly/dd: remove the
     // nonlinear part's share, sum hnl d over the nonlinear features
     for (int e = tid; e < nNL * kNPad; e += kBlock) eacc -= hnl[e] * dnl[e];
+    // the batched units add hnl to the FP32 weights of every tuple: the mixed
+    // path reads an FP32 copy (in the space of dnl, which is no longer read)
+    const R* hnlR = reinterpret_cast<const R*>(hnl);
+    if constexpr (sizeof(R) == 4) {
+      __syncthreads();   // every thread's reads of dnl are done
+      float* hf = reinterpret_cast<float*>(dnl);
+      for (int e = tid; e < nNL * kNPad; e += kBlock) hf[e] = (float)hnl[e];
+      hnlR = reinterpret_cast<const R*>(hf);   // visible after the barrier below
+    }
     MLIPG_STAMP(2)
     // ---------------------------------------------------------------- P5
     // (mixed path: redone once at the measured scale if a flush left the
@@ -1167,19 +1210,20 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     }
     __syncthreads();   // G zeroed; everyone has read this attempt's scale
     GFix gf{sizeof(R) == 4 ? (R)ldexpf(1.0f, gexp) : R(1), R(0)};
+    ESumF esum;   // mixed path: this thread's energy of the statically dealt units
     {
       const int u0 = __ldg(A.unit_off + ti), nU = __ldg(A.unit_off + ti + 1) - u0;
       const int i0 = __ldg(A.iunit_off + ti), nI = __ldg(A.iunit_off + ti + 1) - i0;
       // static round-robin over warps (units are sorted by cost): each
       // thread's energy sum has a fixed order, so energies are reproducible
       const R* wl = wlin_table(A);
-      const auto run_iu = [&](const DeviceIrrUnit& iu, double& e) {
+      const auto run_iu = [&](const DeviceIrrUnit& iu, auto& e) {
         if (T == 3)
-          dispatch_irr<3, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, e);
+          dispatch_irr<3, LS>(iu, A.tuples, A.terms, wl, hnlR, sa, sg, gim, gf, n, half, act, e);
         else if (T == 2)
-          dispatch_irr<2, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, e);
+          dispatch_irr<2, LS>(iu, A.tuples, A.terms, wl, hnlR, sa, sg, gim, gf, n, half, act, e);
         else
-          dispatch_irr<1, LS>(iu, A.tuples, A.terms, wl, hnl, sa, sg, gim, gf, n, half, act, e);
+          dispatch_irr<1, LS>(iu, A.tuples, A.terms, wl, hnlR, sa, sg, gim, gf, n, half, act, e);
       };
       if (A.unit_dyn) {
         // warps take units from a shared counter (no end-of-phase imbalance);
@@ -1192,10 +1236,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           if (lane == 0) u = atomicAdd(misc + 13, 1);
           u = __shfl_sync(0xffffffffu, u, 0);
           if (u >= nI) break;
-          double e = 0.0;
-          run_iu(A.iunits[i0 + u], e);
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+          std::conditional_t<sizeof(R) == 4, ESumF, double> eu{};
+          run_iu(A.iunits[i0 + u], eu);
+          const double e = warp_energy(eu);
           if (lane == 0) {
             const double sc = e * 0x1p20, hi = rint(sc);
             atomicAdd(efix, (unsigned long long)(long long)hi);
@@ -1206,7 +1249,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         for (int u = warp; u < nI; u += kBlock / 32) {
           const DeviceIrrUnit iu = A.iunits[i0 + u];
           if (iu.nterm == 0) continue;   // padding of a balanced schedule
-          run_iu(iu, eacc);
+          if constexpr (sizeof(R) == 4) run_iu(iu, esum);
+          else run_iu(iu, eacc);
         }
       }
       MLIPG_STAMP(3)   // warp 0's batched units (the warps' shares are balanced)
@@ -1252,6 +1296,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       if (out && tid == 0) atomicOr(A.status, kStatusAdjointRange);
       if (A.unit_dyn && tid == 0)
         eacc += unit_energy(misc);
+      eacc += (double)esum.s + (double)esum.c;
       break;
     }
     eacc = eacc0;
