@@ -132,7 +132,8 @@ static int upload_model(mlipg_handle* h) {
   std::vector<DeviceIrrUnit> iunits;
   std::vector<DeviceTuple> tuples;
   std::vector<int> uoff(M.T + 1, 0), noff(M.T + 1, 0), poff(M.T + 1, 0), ioff(M.T + 1, 0);
-  std::vector<int> abase(M.T + 1, 0), adj_off, adj;
+  std::vector<int> abase(M.T + 1, 0), adj_off;
+  std::vector<DeviceAdj> adj;
   for (int t = 0; t < M.T; ++t) {
     const Schedule& S = M.sched[t];
     ioff[t] = (int)iunits.size();
@@ -150,7 +151,16 @@ static int upload_model(mlipg_handle* h) {
     poly.insert(poly.end(), S.poly.begin(), S.poly.end());
     abase[t] = (int)adj_off.size();
     for (int v : S.adj_off) adj_off.push_back((int)adj.size() + v);
-    for (int v : S.adj) adj.push_back((poff[t] + (v >> 2)) * 4 + (v & 3));
+    for (int v : S.adj) {
+      const DevicePoly& dp = S.poly[v >> 2];
+      DeviceAdj a{};
+      a.w = dp.w;
+      int o = 0;
+      for (int q = 0; q < dp.order; ++q)
+        if (q != (v & 3)) a.other[o++] = dp.k[q];
+      for (; o < kMaxPoly - 1; ++o) a.other[o] = -1;
+      adj.push_back(a);
+    }
   }
   ioff[M.T] = (int)iunits.size();
   uoff[M.T] = (int)units.size();
@@ -374,7 +384,7 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.poly_off = h->d_poly_off.as<int>();
   a.adj_base = h->d_adj_base.as<int>();
   a.adj_off = h->d_adj_off.as<int>();
-  a.adj = h->d_adj.as<int>();
+  a.adj = h->d_adj.as<DeviceAdj>();
   a.w_lin = h->d_wlin.as<double>();
   a.w_lin_f = h->d_wlin_f.as<float>();
   a.phase_clocks = h->profiling ? h->d_phase.as<unsigned long long>() : nullptr;
@@ -822,7 +832,7 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
   a.poly_off = h->d_poly_off.as<int>();
   a.adj_base = h->d_adj_base.as<int>();
   a.adj_off = h->d_adj_off.as<int>();
-  a.adj = h->d_adj.as<int>();
+  a.adj = h->d_adj.as<DeviceAdj>();
   a.w_lin = h->d_wlin.as<double>();
   a.w_lin_f = h->d_wlin_f.as<float>();
   a.phase_clocks = h->profiling ? h->d_phase.as<unsigned long long>() : nullptr;

@@ -224,12 +224,12 @@ struct StageVis {
 };
 
 // Stages Y_lm of one neighbour as FP32 pairs for the mixed path's
-// compensated FP32 order-parameter sums.
-struct StageVisF {
+// compensated FP32 order-parameter sums (rows of 2 * kChunk neighbours).
+struct StageVisW {
   float2* ys;
   int slot;
   __device__ __forceinline__ void operator()(int lmh, int, R yre, R yim, R, R, R, R, R, R) {
-    ys[lmh * kChunk + slot] = float2{(float)yre, (float)yim};
+    ys[lmh * (2 * kChunk) + slot] = float2{(float)yre, (float)yim};
   }
 };
 
@@ -1042,53 +1042,58 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       // pipe is some sixty times wider than the FP64 pipe on this GPU.  (At
       // l <= 20 the four accumulators per entry no longer fit in registers
       // beside the rest, so that instantiation keeps the FP64 sums.)
+      // Neighbours are staged in windows of 64 (the FP32 stage takes half the
+      // bytes of the FP64 one), across element boundaries, so one window
+      // usually holds the whole neighbourhood; an element that spans windows
+      // carries its rounded sum from the previous window.
+      constexpr int kWin = 2 * kChunk;
       float2* ysf = reinterpret_cast<float2*>(sg);
-      float* fsf = reinterpret_cast<float*>(smem + lay.g + (size_t)LS * kChunk * sizeof(float2));
+      float* fsf = reinterpret_cast<float*>(smem + lay.g + (size_t)LS * kWin * sizeof(float2));
       const int n = tid & 15;
-      for (int t = 0; t < T; ++t) {
-        float sr[kEPT], cr[kEPT], si[kEPT], ci[kEPT];
+      for (int w0 = 0; w0 < nkeep; w0 += kWin) {
+        const int wsz = min(kWin, nkeep - w0);
+        if (tid < wsz) {
+          const int k = nbk[w0 + tid];
+          const int j = __ldg(A.nbr_idx + k);
+          double dx, dy, dz;
+          pair_disp(A, c, k, xi, A.x4[j], dx, dy, dz);
+          const double r = sqrt(dx * dx + dy * dy + dz * dz);
+          R f[kNPad], fdum[kNPad];
+          radial(A.radial, F, (R)r, rc, f, fdum, false);
 #pragma unroll
-        for (int e = 0; e < kEPT; ++e) { sr[e] = 0.f; cr[e] = 0.f; si[e] = 0.f; ci[e] = 0.f; }
-        const int b0 = misc[t], b1 = misc[t + 1];
-        for (int cb = b0; cb < b1; cb += kChunk) {
-          const int csz = min(kChunk, b1 - cb);
-          if (tid < csz) {
-            const int k = nbk[cb + tid];
-            const int j = __ldg(A.nbr_idx + k);
-            double dx, dy, dz;
-            pair_disp(A, c, k, xi, A.x4[j], dx, dy, dz);
-            const double r = sqrt(dx * dx + dy * dy + dz * dz);
-            R f[kNPad], fdum[kNPad];
-            radial(A.radial, F, (R)r, rc, f, fdum, false);
-#pragma unroll
-            for (int q = 0; q < kNPad; ++q) fsf[tid * kNPad + q] = (float)f[q];
-            StageVisF v{ysf, tid};
-            sh_visit<LCAP, false>((R)dx, (R)dy, (R)dz, (R)r, L, v);
-          }
-          __syncthreads();
+          for (int q = 0; q < kNPad; ++q) fsf[tid * kNPad + q] = (float)f[q];
+          StageVisW v{ysf, tid};
+          sh_visit<LCAP, false>((R)dx, (R)dy, (R)dz, (R)r, L, v);
+        }
+        __syncthreads();
+        for (int t = 0; t < T; ++t) {
+          const int j0 = max(misc[t], w0), j1 = min(misc[t + 1], w0 + wsz);
+          if (j0 >= j1) continue;
+          const bool cont = misc[t] < w0;
 #pragma unroll
           for (int e = 0; e < kEPT; ++e) {
+            const int idx = tid + e * kBlock;
+            const int lmh = idx >> 4;
+            Rc* dst = sa + (t * LS + lmh) * kNPad + (idx & 15);
+            float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+            if (cont && lmh < Lh) { sr = dst->x; si = dst->y; }
             // rows past Lh read a staged row and are never stored
-            const float2* yrow = ysf + min((tid + e * kBlock) >> 4, Lh - 1) * kChunk;
+            const float2* yrow = ysf + min(lmh, Lh - 1) * kWin;
 #pragma unroll 4
-            for (int jj = 0; jj < csz; ++jj) {
+            for (int jj = j0 - w0; jj < j1 - w0; ++jj) {
               const float fv = fsf[jj * kNPad + n];
               const float2 y = yrow[jj];
-              two_sum_acc(sr[e], cr[e], __fmul_rn(fv, y.x));
-              two_sum_acc(si[e], ci[e], __fmul_rn(-fv, y.y));
+              two_sum_acc(sr, cr, __fmul_rn(fv, y.x));
+              two_sum_acc(si, ci, __fmul_rn(-fv, y.y));
             }
+            if (lmh < Lh) *dst = Rc{(R)__fadd_rn(sr, cr), (R)__fadd_rn(si, ci)};
           }
-          __syncthreads();
         }
-#pragma unroll
-        for (int e = 0; e < kEPT; ++e) {
-          const int idx = tid + e * kBlock;
-          const int lmh = idx >> 4;
-          if (lmh < Lh)
-            sa[(t * LS + lmh) * kNPad + (idx & 15)] =
-                Rc{(R)__fadd_rn(sr[e], cr[e]), (R)__fadd_rn(si[e], ci[e])};
-        }
+        __syncthreads();
       }
+      for (int t = 0; t < T; ++t)   // elements without neighbours
+        if (misc[t] == misc[t + 1])
+          for (int idx = tid; idx < Lh * kNPad; idx += kBlock) sa[t * LS * kNPad + idx] = Rc{R(0), R(0)};
     } else
     for (int t = 0; t < T; ++t) {
       double accr[kEPT], acci[kEPT];
@@ -1151,6 +1156,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       }
       __syncthreads();
       const int p0 = __ldg(A.poly_off + ti), np = __ldg(A.poly_off + ti + 1) - p0;
+#pragma unroll 4
       for (int pt = tid; pt < np; pt += kBlock) {
         const DevicePoly dp = A.poly[p0 + pt];
         double v[kMaxPoly];
@@ -1163,21 +1169,39 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         eacc += dp.w * prod;
       }
       // dE_poly/dd per nonlinear entry, gathered in a fixed order (no atomics,
-      // so the energies that weigh products with H stay reproducible)
+      // so the energies that weigh products with H stay reproducible).  With
+      // few entries each one's list is cut into S contiguous slices summed by
+      // S threads (partials in the G space, free until the adjoint phase) and
+      // the slices are added in slice order.
       const int ab = __ldg(A.adj_base + ti);
-      for (int e = tid; e < nNL * kNPad; e += kBlock) {
+      const int ne = nNL * kNPad;
+      const int S = ne >= kBlock ? 1 : kBlock / ne;
+      double* part = reinterpret_cast<double*>(sg);
+      for (int w = tid; w < ne * S; w += kBlock) {
+        const int e = w % ne, sl = w / ne;
+        const int x0 = __ldg(A.adj_off + ab + e), len = __ldg(A.adj_off + ab + e + 1) - x0;
+        const int xs = x0 + (len * sl) / S, xe = x0 + (len * (sl + 1)) / S;
         double h = 0.0;
-        const int x1 = __ldg(A.adj_off + ab + e + 1);
-        for (int x = __ldg(A.adj_off + ab + e); x < x1; ++x) {
-          const int v = __ldg(A.adj + x);
-          const DevicePoly dp = A.poly[v >> 2];
-          double o = dp.w;
+#pragma unroll 4
+        for (int x = xs; x < xe; ++x) {
+          const DeviceAdj a = A.adj[x];
+          double o = a.w;
 #pragma unroll
-          for (int q2 = 0; q2 < kMaxPoly; ++q2)
-            if (q2 != (v & 3) && q2 < dp.order) o *= dnl[dp.k[q2]];
+          for (int q2 = 0; q2 < kMaxPoly - 1; ++q2)
+            if (a.other[q2] >= 0) o *= dnl[a.other[q2]];
           h += o;
         }
-        hnl[e] = h;
+        if (S == 1) hnl[e] = h;
+        else part[w] = h;
+      }
+      if (S > 1) {
+        __syncthreads();
+        for (int e = tid; e < ne; e += kBlock) {
+          double h = 0.0;
+          for (int sl = 0; sl < S; ++sl) h += part[sl * ne + e];
+          hnl[e] = h;
+        }
+        __syncthreads();   // partials read before the adjoint phase clears G
       }
     }
     // ---------------------------------------------------------------- P4

@@ -42,7 +42,7 @@ struct KernelArgs {
   const int* poly_off;    // [T + 1]
   const int* adj_base;    // [T]: first entry of each element's adj_off rows
   const int* adj_off;     // polynomial adjoint gather lists (global CSR)
-  const int* adj;         // global poly index * 4 + factor
+  const DeviceAdj* adj;   // (term weight, other factors) per gather entry
   const double* w_lin;    // [n_itc][16]
   const float* w_lin_f;   // [n_itc][16], FP32 copy for the mixed path
   const double* radial;   // [F][2] (beta, mu)

@@ -67,6 +67,14 @@ struct DevicePoly {       // 32 bytes
   int pad;
 };
 
+// One (polynomial term, factor) pair of the adjoint gather, flattened so that
+// the kernel reads one record per pair: dE/dd_k += w * prod(d[other])
+struct DeviceAdj {        // 32 bytes
+  double w;               // the term's weight
+  int other[kMaxPoly - 1];  // the term's other factors (slot*16 + n), -1 past its order
+  int pad[3];
+};
+
 // Element tuples of one irreps (orders 1..4, up to 3 elements) over a chunk
 // of its canonical terms.  Order-4 units fix the element of slot 0 (s0) and
 // cover the T^3 tuples of the other slots; lower orders cover all T^q tuples;
