@@ -472,6 +472,18 @@ __device__ __forceinline__ const R* wlin_table(const KernelArgs& A) {
 // slot's partials (sum_j H_j Pi_j = sum_s g_last[s] a_last[s]).  Shorter
 // dependency chains than the factorized form, which pays off only with
 // three elements.
+// Weight H = w + dE_poly/dd of one tuple at channel n (0 for a non-feature
+// tuple or an idle lane).  Both loads are issued unconditionally from clamped
+// rows (row 0 always exists; the nonlinear row n < 16 lies inside shared
+// memory) so the unrolled setup of a unit issues all its loads at once.
+__device__ __forceinline__ R tuple_weight(int2 e, const R* __restrict__ wlin, const R* hnl, int n,
+                                          bool act) {
+  const R w = __ldg(wlin + (size_t)max(e.x, 0) * kNPad + n);
+  const R hn = hnl[max(e.y, 0) * kNPad + n];
+  const R h = e.y >= 0 ? w + hn : w;
+  return (act && e.x >= 0) ? h : R(0);
+}
+
 template <int Q, int TT, int Lh, class EA>
 __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
@@ -485,12 +497,7 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
 #pragma unroll
   for (int j = 0; j < NT; ++j) {
     const int2 e = __ldg(reinterpret_cast<const int2*>(tups + u.tup + j));
-    R h = R(0);
-    if (act && e.x >= 0) {
-      h = __ldg(wlin + (size_t)e.x * kNPad + n);
-      if (e.y >= 0) h += hnl[e.y * kNPad + n];
-    }
-    H[j] = h;
+    H[j] = tuple_weight(e, wlin, hnl, n, act);
   }
   // Energy: sum_j H_j d_j of this unit's tuples, formed per term from the
   // last slot's adjoint partial (sum_j H_j Pi_j = sum_s g_last[s] a_last[s]);
@@ -665,12 +672,7 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       for (int y = 0; y < NY; ++y) {
         const int2 e =
             __ldg(reinterpret_cast<const int2*>(tups + u.tup + (z * NX + x) * NY + y));
-        R h = R(0);
-        if (act && e.x >= 0) {
-          h = __ldg(wlin + (size_t)e.x * kNPad + n);
-          if (e.y >= 0) h += hnl[e.y * kNPad + n];
-        }
-        H[z][x][y] = h;
+        H[z][x][y] = tuple_weight(e, wlin, hnl, n, act);
       }
   const int s0 = (int)u.s0;
   constexpr int es = Lh * kNPad;   // element stride in the a / G arrays
@@ -1255,19 +1257,41 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         // integer parts and added to two 64-bit sums, so the total does not
         // depend on which warp ran which unit
         unsigned long long* efix = reinterpret_cast<unsigned long long*>(misc + 24);
-        for (;;) {
-          int u = 0;
-          if (lane == 0) u = atomicAdd(misc + 13, 1);
-          u = __shfl_sync(0xffffffffu, u, 0);
-          if (u >= nI) break;
+        // the next unit is taken before the current one runs, and its
+        // descriptor copied asynchronously (cp.async, no registers held) into
+        // this warp's slot of the block-reduction space, unused until the end
+        // of the centre
+        DeviceIrrUnit* slot = reinterpret_cast<DeviceIrrUnit*>(red) + 2 * warp;
+        const auto take = [&]() {
+          int v = 0;
+          if (lane == 0) v = atomicAdd(misc + 13, 1);
+          return __shfl_sync(0xffffffffu, v, 0);
+        };
+        const auto fetch = [&](int v) {
+          if (lane == 0 && v < nI) {
+            const unsigned sa_ = (unsigned)__cvta_generic_to_shared(slot);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n\tcp.async.commit_group;" ::"r"(sa_),
+                         "l"(A.iunits + i0 + v) : "memory");
+          }
+        };
+        int u = take();
+        fetch(u);
+        while (u < nI) {
+          if (lane == 0) asm volatile("cp.async.wait_all;" ::: "memory");
+          __syncwarp();
+          const DeviceIrrUnit cur = *slot;
+          __syncwarp();   // every lane has read the slot before it is refilled
+          const int un = take();
+          fetch(un);
           std::conditional_t<sizeof(R) == 4, ESumF, double> eu{};
-          run_iu(A.iunits[i0 + u], eu);
+          run_iu(cur, eu);
           const double e = warp_energy(eu);
           if (lane == 0) {
             const double sc = e * 0x1p20, hi = rint(sc);
             atomicAdd(efix, (unsigned long long)(long long)hi);
             atomicAdd(efix + 1, (unsigned long long)__double2ll_rn((sc - hi) * 0x1p40));
           }
+          u = un;
         }
       } else {
         for (int u = warp; u < nI; u += kBlock / 32) {
