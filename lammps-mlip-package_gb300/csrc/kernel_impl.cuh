@@ -966,12 +966,14 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     const int o0 = __ldg(A.nbr_off + c), o1 = __ldg(A.nbr_off + c + 1);
     if (prof && tid == 0) tstamp = clock64();
     // ---------------------------------------------------------------- P1
-    if (warp == 0) {
-      int cnt[kMaxTypes];
-#pragma unroll
-      for (int t = 0; t < kMaxTypes; ++t) cnt[t] = 0;
-      for (int base = o0; base < o1; base += 32) {
-        const int k = base + lane;
+    // Neighbour compaction.  Each warp classifies a contiguous range of
+    // 32-entry chunks of the list (inside the cutoff, element); the per-(warp,
+    // element) counts meet in shared memory (the block-reduction space, free
+    // until the end of the centre) and each warp scatters its entries after
+    // the elements before and the warps before it, which gives the serial
+    // order: element-major, list order within an element.
+    {
+      const auto classify = [&](int k) {
         int t = -1;
         if (k < o1) {
           const int j = __ldg(A.nbr_idx + k);
@@ -982,51 +984,67 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           t = (int)xj.w;
           if (!(t >= 0 && t < T && r2 <= rc2 && r2 > 0.0)) t = -1;
         }
+        return t;
+      };
+      int* wcnt = reinterpret_cast<int*>(red);   // [warp][kMaxTypes]
+      const int nch = (o1 - o0 + 31) >> 5;
+      const int cpw = (nch + kBlock / 32 - 1) / (kBlock / 32);
+      const int ch0 = warp * cpw, ch1 = min(nch, ch0 + cpw);
+      int t0 = -1;   // class of this lane's entry in the warp's first chunk
+      {
+        int cnt[kMaxTypes];
+#pragma unroll
+        for (int t = 0; t < kMaxTypes; ++t) cnt[t] = 0;
+        for (int ch = ch0; ch < ch1; ++ch) {
+          const int t = classify(o0 + 32 * ch + lane);
+          if (ch == ch0) t0 = t;
+#pragma unroll
+          for (int tt = 0; tt < kMaxTypes; ++tt)
+            if (tt < T) cnt[tt] += __popc(__ballot_sync(0xffffffffu, t == tt));
+        }
 #pragma unroll
         for (int tt = 0; tt < kMaxTypes; ++tt)
-          if (tt < T) cnt[tt] += __popc(__ballot_sync(0xffffffffu, t == tt));
+          if (lane == tt) wcnt[warp * kMaxTypes + tt] = cnt[tt];
       }
-      int tot = 0, toff[kMaxTypes + 1];
+      __syncthreads();
+      if (ch0 < ch1 || warp == 0) {
+        int tot = 0, toff[kMaxTypes + 1], cur[kMaxTypes];
 #pragma unroll
-      for (int tt = 0; tt < kMaxTypes; ++tt) {
-        toff[tt] = tot;
-        if (tt < T) tot += cnt[tt];
-      }
-      toff[kMaxTypes] = tot;
-      const bool over = tot > A.nb_cap;
-      if (!over) {
-        int cur[kMaxTypes];
-#pragma unroll
-        for (int tt = 0; tt < kMaxTypes; ++tt) cur[tt] = toff[tt];
-        const unsigned lt = (1u << lane) - 1u;
-        for (int base = o0; base < o1; base += 32) {
-          const int k = base + lane;
-          int t = -1;
-          if (k < o1) {
-            const int j = __ldg(A.nbr_idx + k);
-            const double4 xj = A.x4[j];
-            double dx, dy, dz;
-            pair_disp(A, c, k, xi, xj, dx, dy, dz);
-            const double r2 = dx * dx + dy * dy + dz * dz;
-            t = (int)xj.w;
-            if (!(t >= 0 && t < T && r2 <= rc2 && r2 > 0.0)) t = -1;
-          }
-#pragma unroll
-          for (int tt = 0; tt < kMaxTypes; ++tt) {
-            if (tt < T) {
-              const unsigned b = __ballot_sync(0xffffffffu, t == tt);
-              if (t == tt) nbk[cur[tt] + __popc(b & lt)] = k;
-              cur[tt] += __popc(b);
+        for (int tt = 0; tt < kMaxTypes; ++tt) {
+          toff[tt] = tot;
+          cur[tt] = tot;
+          if (tt < T) {
+            for (int w = 0; w < kBlock / 32; ++w) {
+              const int v = wcnt[w * kMaxTypes + tt];
+              if (w < warp) cur[tt] += v;
+              tot += v;
             }
           }
         }
-      }
-      if (lane == 0) {
+        toff[kMaxTypes] = tot;
+        const bool over = tot > A.nb_cap;
+        if (!over) {
+          const unsigned lt = (1u << lane) - 1u;
+          for (int ch = ch0; ch < ch1; ++ch) {
+            const int k = o0 + 32 * ch + lane;
+            const int t = ch == ch0 ? t0 : classify(k);
 #pragma unroll
-        for (int tt = 0; tt <= kMaxTypes; ++tt) misc[tt] = tt < T ? toff[tt] : tot;
-        misc[9] = over ? 1 : 0;
-        misc[10] = 0;
-        if (over) atomicOr(A.status, kStatusNeighbourCapacity);
+            for (int tt = 0; tt < kMaxTypes; ++tt) {
+              if (tt < T) {
+                const unsigned b = __ballot_sync(0xffffffffu, t == tt);
+                if (t == tt) nbk[cur[tt] + __popc(b & lt)] = k;
+                cur[tt] += __popc(b);
+              }
+            }
+          }
+        }
+        if (tid == 0) {
+#pragma unroll
+          for (int tt = 0; tt <= kMaxTypes; ++tt) misc[tt] = tt < T ? toff[tt] : tot;
+          misc[9] = over ? 1 : 0;
+          misc[10] = 0;
+          if (over) atomicOr(A.status, kStatusNeighbourCapacity);
+        }
       }
     }
     __syncthreads();
