@@ -113,6 +113,28 @@ def test_workload_potentials(tmp_path, name):
     assert abs(mix["energy"] - ref["energy"]) / s.nlocal <= 1e-6
 
 
+@pytest.mark.parametrize("name", ["fcc-ternary-1m", "fcc-al-256"])
+def test_dense_neighbourhoods(tmp_path, name):
+    """Compressed fcc (a = 3.3 A, about 100 neighbours inside 6 A): the mixed
+    path stages the order-parameter sums in windows of 64 neighbours, so here
+    every neighbourhood spans two windows and elements straddle the boundary."""
+    rng = np.random.default_rng(11)
+    path = str(tmp_path / (name + ".mlip"))
+    workload_potential(path, name, seed=5)
+    cell = jitter(fcc_cell(3, 3, 3, 3.3), 0.05, rng)
+    o = Oracle(path, threads=16)
+    if o.info["T"] > 1:
+        cell = random_types(cell, o.info["T"], rng)
+    s = build_system(cell, o.cutoff, skin=1.0)
+    ref = o.compute(s)
+    got = mlipg.Potential(path, mlipg.PREC_FP64).compute(s)
+    check_fp64(got, ref, s)
+    mix = mlipg.Potential(path, mlipg.PREC_MIXED).compute(s)
+    F, Fr = s.fold_forces(mix["f_all"]), s.fold_forces(ref["f_all"])
+    assert np.sqrt(np.mean((F - Fr) ** 2)) <= 1e-4
+    assert abs(mix["energy"] - ref["energy"]) / s.nlocal <= 1e-6
+
+
 def test_edge_cases(potdir):
     g = mlipg.Potential(potdir["gtinv-820"], mlipg.PREC_FP64)
     o = Oracle(potdir["gtinv-820"])
