@@ -39,9 +39,15 @@ enum mlipg_status {
 };
 
 enum mlipg_precision {
-  MLIPG_PREC_FP64 = 0, /* every product and sum in FP64 (plain path) */
-  MLIPG_PREC_MIXED = 1 /* FP32 radial/Y_lm/invariant/adjoint products;
-                          FP64 order-parameter sums, force, energy, virial */
+  MLIPG_PREC_FP64 = 0,      /* every product and sum in FP64 (plain path) */
+  MLIPG_PREC_MIXED = 1,     /* FP32 radial/Y_lm/invariant/adjoint products;
+                               order-parameter neighbour sums and unit energies
+                               in FP32 with TwoSum compensation (error terms
+                               kept exactly, FP64-grade accumulation at FP32
+                               pipe speed); force, per-atom and total energy
+                               and virial accumulation in FP64 */
+  MLIPG_PREC_MIXED_A64 = 2  /* as MLIPG_PREC_MIXED, with the order-parameter
+                               neighbour sums made with plain FP64 FMAs */
 };
 
 /* Message of the last failure on this handle (h may be NULL for failures
@@ -58,7 +64,7 @@ int mlipg_create(const char* potential_path, int precision, mlipg_handle** out);
  * pair_mlip_gtinv_kokkos_impl.h:60-85) */
 int mlipg_destroy(mlipg_handle* h);
 
-/* Switches between MLIPG_PREC_FP64 and MLIPG_PREC_MIXED. */
+/* Switches between MLIPG_PREC_FP64, MLIPG_PREC_MIXED and MLIPG_PREC_MIXED_A64. */
 int mlipg_set_precision(mlipg_handle* h, int precision);
 
 /* Elements of the potential file, their masses and the cutoff radius.

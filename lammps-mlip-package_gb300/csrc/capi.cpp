@@ -214,7 +214,7 @@ const char* mlipg_last_error(const mlipg_handle* h) {
 int mlipg_create(const char* path, int precision, mlipg_handle** out) {
   if (!out || !path) return fail(nullptr, MLIPG_EINVAL, "mlipg_create: null argument");
   *out = nullptr;
-  if (precision != MLIPG_PREC_FP64 && precision != MLIPG_PREC_MIXED)
+  if (precision < MLIPG_PREC_FP64 || precision > MLIPG_PREC_MIXED_A64)
     return fail(nullptr, MLIPG_EINVAL, "unknown precision %d", precision);
   mlipg_handle* h = new mlipg_handle();
   h->precision = precision;
@@ -287,7 +287,7 @@ int mlipg_destroy(mlipg_handle* h) {
 
 int mlipg_set_precision(mlipg_handle* h, int precision) {
   if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
-  if (precision != MLIPG_PREC_FP64 && precision != MLIPG_PREC_MIXED)
+  if (precision < MLIPG_PREC_FP64 || precision > MLIPG_PREC_MIXED_A64)
     return fail(h, MLIPG_EINVAL, "unknown precision %d", precision);
   h->precision = precision;
   return MLIPG_OK;
@@ -398,6 +398,7 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.rc = M.pot.cutoff;
   a.g_bound = (float)M.g_bound;
   a.unit_dyn = M.tiling.warp_order == 2 ? 1 : 0;
+  a.sum64 = h->precision == MLIPG_PREC_MIXED_A64 ? 1 : 0;
   a.f = f;
   a.eatom = eatom;
   a.vatom = vatom;
@@ -846,6 +847,7 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
   a.rc = M.pot.cutoff;
   a.g_bound = (float)M.g_bound;
   a.unit_dyn = M.tiling.warp_order == 2 ? 1 : 0;
+  a.sum64 = h->precision == MLIPG_PREC_MIXED_A64 ? 1 : 0;
   a.f = d_f;
   a.eatom = d_eatom;
   a.vatom = d_vatom;

@@ -1056,12 +1056,13 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     const int nkeep = misc[T];
     MLIPG_STAMP(0)
     // ---------------------------------------------------------------- P2
-    if constexpr (sizeof(R) == 4 && LCAP <= 16) {
+    if (sizeof(R) == 4 && LCAP <= 16 && !A.sum64) {
       // Mixed path: FP32 products summed with TwoSum compensation (sum and
       // error term per entry), rounded once to FP32 at the end; the FP32
       // pipe is some sixty times wider than the FP64 pipe on this GPU.  (At
       // l <= 20 the four accumulators per entry no longer fit in registers
-      // beside the rest, so that instantiation keeps the FP64 sums.)
+      // beside the rest, so that instantiation keeps the FP64 sums, as does
+      // the precision that asks for them.)
       // Neighbours are staged in windows of 64 (the FP32 stage takes half the
       // bytes of the FP64 one), across element boundaries, so one window
       // usually holds the whole neighbourhood; an element that spans windows

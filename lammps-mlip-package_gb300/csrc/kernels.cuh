@@ -50,6 +50,7 @@ struct KernelArgs {
   double rc;
   float g_bound;          // mixed path: largest fixed-point adjoint flush (power of two)
   int unit_dyn;           // 1: warps take batched units from a shared counter
+  int sum64;              // mixed path: order-parameter sums in plain FP64 FMAs
   // outputs
   double* f;              // [nforce][3], accumulated with atomics
   double* eatom;          // [ncenters] (may be null)

@@ -52,7 +52,7 @@ void PairMLIPGtinvGPU::allocate()
     for (int j = i; j <= n; j++) setflag[i][j] = 0;
 }
 
-// pair_style mlip_gtinv/gpu [fp64|mixed]  (the reference takes no arguments,
+// pair_style mlip_gtinv/gpu [fp64|mixed|mixed_a64]  (the reference takes no arguments,
 // pair_mlip_gtinv_kokkos_impl.h:87-90; the optional keyword selects precision)
 void PairMLIPGtinvGPU::settings(int narg, char **arg)
 {
@@ -60,6 +60,7 @@ void PairMLIPGtinvGPU::settings(int narg, char **arg)
   if (narg == 1) {
     if (strcmp(arg[0], "fp64") == 0) precision = MLIPG_PREC_FP64;
     else if (strcmp(arg[0], "mixed") == 0) precision = MLIPG_PREC_MIXED;
+    else if (strcmp(arg[0], "mixed_a64") == 0) precision = MLIPG_PREC_MIXED_A64;
     else error->all(FLERR, "Illegal pair_style command");
   }
 }

@@ -18,6 +18,7 @@ from . import build as _build
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_MIXED_A64 = 2   # mixed, with the order-parameter sums in plain FP64
 ERRORS = {1: "EINVAL", 2: "EIO", 3: "ENOMEM", 4: "ECUDA", 5: "ENOTSUP", 6: "ECAPACITY",
           7: "ENOGPU", 8: "ETIMEDOUT", 9: "EBUSY"}
 

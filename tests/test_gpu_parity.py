@@ -135,6 +135,28 @@ def test_dense_neighbourhoods(tmp_path, name):
     assert abs(mix["energy"] - ref["energy"]) / s.nlocal <= 1e-6
 
 
+@pytest.mark.parametrize("name", ["bcc-binary-16k", "fcc-ternary-1m", "triclinic-batch"])
+def test_mixed_fp64_sums(tmp_path, name):
+    """MLIPG_PREC_MIXED_A64 (order-parameter sums in plain FP64) meets the
+    mixed bounds against the oracle, and the compensated FP32 sums of
+    MLIPG_PREC_MIXED agree with it to far inside them."""
+    rng = np.random.default_rng(7)
+    path = str(tmp_path / (name + ".mlip"))
+    workload_potential(path, name, seed=3)
+    cell = workload_system(name, rng)
+    o = Oracle(path, threads=16)
+    s = build_system(cell, o.cutoff, skin=1.0)
+    ref = o.compute(s)
+    a64 = mlipg.Potential(path, mlipg.PREC_MIXED_A64).compute(s)
+    mix = mlipg.Potential(path, mlipg.PREC_MIXED).compute(s)
+    Fr = s.fold_forces(ref["f_all"])
+    Fa, Fm = s.fold_forces(a64["f_all"]), s.fold_forces(mix["f_all"])
+    assert np.sqrt(np.mean((Fa - Fr) ** 2)) <= 1e-4
+    assert abs(a64["energy"] - ref["energy"]) / s.nlocal <= 1e-6
+    assert np.sqrt(np.mean((Fm - Fa) ** 2)) <= 1e-6
+    assert abs(mix["energy"] - a64["energy"]) / s.nlocal <= 1e-8
+
+
 def test_edge_cases(potdir):
     g = mlipg.Potential(potdir["gtinv-820"], mlipg.PREC_FP64)
     o = Oracle(potdir["gtinv-820"])
