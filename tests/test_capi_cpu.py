@@ -72,6 +72,23 @@ def test_type_map_semantics(potdir):
         p.set_type_map(["NULL", "NULL"])
 
 
+def test_precision_values(potdir):
+    """The three precisions are accepted at creation and by set_precision;
+    anything else is EINVAL and leaves the handle as it was."""
+    for prec in (mlipg.PREC_FP64, mlipg.PREC_MIXED, mlipg.PREC_MIXED_A64):
+        p = mlipg.Potential(potdir["gtinv-434"], prec)
+        p.set_precision(mlipg.PREC_MIXED_A64)
+        p.set_precision(prec)
+        for bad in (-1, 3):
+            with pytest.raises(mlipg.MlipgError) as e:
+                p.set_precision(bad)
+            assert e.value.code == 1
+        p.close()
+    with pytest.raises(mlipg.MlipgError) as e:
+        mlipg.Potential(potdir["gtinv-434"], 3)
+    assert e.value.code == 1
+
+
 def test_bad_potential_files(tmp_path):
     with pytest.raises(mlipg.MlipgError) as e:
         mlipg.Potential(str(tmp_path / "missing.mlip"))
