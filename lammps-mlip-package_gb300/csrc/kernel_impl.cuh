@@ -379,7 +379,7 @@ __device__ __forceinline__ void gput(R* p, R y, GFix& g, int lo) {
     const float th = fmaf(y, 1.0f / 65536.0f, 12582912.0f);   // rint(y / 2^16) + 1.5 * 2^23
     const float yl = fmaf(-(th - 12582912.0f), 65536.0f, y);  // y - hi * 2^16, exact
     atomicAdd(reinterpret_cast<int*>(p), __float_as_int(th) - 0x4B400000);
-    atomicAdd(reinterpret_cast<int*>(p) + lo, __float_as_int(yl + 12582912.0f) - 0x4B400000);
+    atomicAdd(reinterpret_cast<int*>(p) + lo, __float2int_rn(yl));   // |yl| <= 2^15 + 1/2
   } else {
     atomicAdd(p, y);
   }
