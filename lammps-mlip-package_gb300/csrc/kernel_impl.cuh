@@ -3,10 +3,12 @@
 // One CTA evaluates one centre atom at a time (persistent grid-stride loop
 // over centres); every intermediate of the reference's seven stages stays in
 // shared memory:
-//   P1  neighbour compaction: keep r <= rc, stable-sort by element (warp 0)
+//   P1  neighbour compaction: keep r <= rc, stable-sort by element (all
+//       warps, per-warp counts and a prefix keep the list order)
 //   P2  order parameters a[s][lm][n] = sum_j f_n(r) conj(Y_lm): f_n and Y_lm
-//       evaluated in REAL; FP64 path: staged as FP64 and summed with FP64
-//       FMAs; mixed path: FP32 products summed with TwoSum compensation
+//       evaluated in REAL; FP64 path (and the mixed precision that asks
+//       for FP64 sums): staged as FP64 and summed with FP64 FMAs; mixed
+//       path: FP32 products summed with TwoSum compensation
 //       (mlipkk_lmp.h:314-387, mlipkk_features_kk.h:9-48,
 //       mlipkk_spherical_harmonics_kk.h:18-81)
 //   P3  nonlinear features and polynomial terms of order >= 2: energy part
@@ -1259,8 +1261,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     {
       const int u0 = __ldg(A.unit_off + ti), nU = __ldg(A.unit_off + ti + 1) - u0;
       const int i0 = __ldg(A.iunit_off + ti), nI = __ldg(A.iunit_off + ti + 1) - i0;
-      // static round-robin over warps (units are sorted by cost): each
-      // thread's energy sum has a fixed order, so energies are reproducible
+      // warp orders 0 and 1 deal the units to the warps statically (each
+      // thread's energy sum has a fixed order, so energies are reproducible);
+      // order 2 hands them out from a shared counter (below)
       const R* wl = wlin_table(A);
       const auto run_iu = [&](const DeviceIrrUnit& iu, auto& e) {
         if (T == 3)
