@@ -8,7 +8,7 @@
 //   P2  order parameters a[s][lm][n] = sum_j f_n(r) conj(Y_lm): f_n and Y_lm
 //       evaluated in REAL; FP64 path (and the mixed precision that asks
 //       for FP64 sums): staged as FP64 and summed with FP64 FMAs; mixed
-//       path: FP32 products summed with TwoSum compensation
+//       path: FP32 products summed with Kahan compensation
 //       (mlipkk_lmp.h:314-387, mlipkk_features_kk.h:9-48,
 //       mlipkk_spherical_harmonics_kk.h:18-81)
 //   P3  nonlinear features and polynomial terms of order >= 2: energy part
@@ -243,6 +243,16 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float p) {
   const float bp = __fsub_rn(t, s);
   const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
   c = __fadd_rn(c, e);
+  s = t;
+}
+
+// s - c += a * b with Kahan's compensated summation, the product fused into
+// the compensating FMA (c holds the negated part that the last addition lost;
+// the value of the pair is s - c).
+__device__ __forceinline__ void kahan_fma_acc(float& s, float& c, float a, float b) {
+  const float y = __fmaf_rn(a, b, -c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
   s = t;
 }
 
@@ -1059,8 +1069,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     MLIPG_STAMP(0)
     // ---------------------------------------------------------------- P2
     if (sizeof(R) == 4 && LCAP <= 16 && !A.sum64) {
-      // Mixed path: FP32 products summed with TwoSum compensation (sum and
-      // error term per entry), rounded once to FP32 at the end; the FP32
+      // Mixed path: FP32 products summed with Kahan compensation (sum and
+      // compensation term per entry), rounded once to FP32 at the end; the FP32
       // pipe is some sixty times wider than the FP64 pipe on this GPU.  (At
       // l <= 20 the four accumulators per entry no longer fit in registers
       // beside the rest, so that instantiation keeps the FP64 sums, as does
@@ -1106,10 +1116,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
             for (int jj = j0 - w0; jj < j1 - w0; ++jj) {
               const float fv = fsf[jj * kNPad + n];
               const float2 y = yrow[jj];
-              two_sum_acc(sr, cr, __fmul_rn(fv, y.x));
-              two_sum_acc(si, ci, __fmul_rn(-fv, y.y));
+              kahan_fma_acc(sr, cr, fv, y.x);
+              kahan_fma_acc(si, ci, -fv, y.y);
             }
-            if (lmh < Lh) *dst = Rc{(R)__fadd_rn(sr, cr), (R)__fadd_rn(si, ci)};
+            if (lmh < Lh) *dst = Rc{(R)__fsub_rn(sr, cr), (R)__fsub_rn(si, ci)};
           }
         }
         __syncthreads();
