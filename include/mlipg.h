@@ -41,10 +41,9 @@ enum mlipg_status {
 enum mlipg_precision {
   MLIPG_PREC_FP64 = 0,      /* every product and sum in FP64 (plain path) */
   MLIPG_PREC_MIXED = 1,     /* FP32 radial/Y_lm/invariant/adjoint products;
-                               order-parameter neighbour sums and unit energies
-                               in FP32 with TwoSum compensation (error terms
-                               kept exactly, FP64-grade accumulation at FP32
-                               pipe speed); force, per-atom and total energy
+                               order-parameter neighbour sums (Kahan) and unit
+                               energies (TwoSum) in compensated FP32, at FP32
+                               pipe speed; force, per-atom and total energy
                                and virial accumulation in FP64 */
   MLIPG_PREC_MIXED_A64 = 2  /* as MLIPG_PREC_MIXED, with the order-parameter
                                neighbour sums made with plain FP64 FMAs */
