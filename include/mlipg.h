@@ -251,8 +251,9 @@ int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4, const int* d
 /* Serving: energy + force + stress requests for periodic structures of any
  * size, evaluated by continuous batching.  Requests (mlipg_server_submit,
  * thread-safe) are admitted in arrival order against a device-memory budget,
- * grouped by precision into batches of at most max_batch_atoms atoms and
- * launched as they arrive; FP64 and mixed batches run on separate streams.
+ * grouped by precision (MLIPG_PREC_FP64 or MLIPG_PREC_MIXED; other values are
+ * MLIPG_EINVAL) into batches of at most max_batch_atoms atoms and launched as
+ * they arrive; FP64 and mixed batches run on separate streams.
  * mlipg_server_wait returns a request's energy, forces[natoms*3] and virial
  * (LAMMPS order) or MLIPG_ETIMEDOUT at its deadline.  A request's energy
  * does not depend on the other requests in its batch.
