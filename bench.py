@@ -75,6 +75,7 @@ POT_DESC = {
                        "model_type 3 max_p 2, 11805 coefficients ~N(0,1e-3)",
 }
 SKIN = 1.0
+PRECISIONS = {"mixed": 1, "fp64": 0, "mixed_a64": 2}   # mlipg.PREC_* values
 
 
 def make_cell(spec, n=None, seed=1):
@@ -281,7 +282,7 @@ def run_ours(args, dist):
         if rank == 0 and args.cpu_seconds > 0 else None
 
     dev = torch.device("cuda", 0)
-    g = mlipg.Potential(pot, mlipg.PREC_MIXED)
+    g = mlipg.Potential(pot, PRECISIONS[args.precision])
     stream = torch.cuda.ExternalStream(g.stream(), device=dev)
     x4 = np.zeros((sysm.nall, 4))
     x4[:, :3] = sysm.x
@@ -349,7 +350,8 @@ def run_ours(args, dist):
     if args.device_only:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "partial": True,
-                              "config": {"workload": args.workload, "centres": ncent_main},
+                              "config": {"workload": args.workload, "centres": ncent_main,
+                                         "precision": args.precision},
                               "kernel_ms_per_launch": ktimes, "phase_share": phase_share,
                               "clocks": clk}), flush=True)
         g.close()
@@ -831,9 +833,14 @@ def main():
                     help="keep the default tile shape instead of autotuning it")
     ap.add_argument("--tiling", default="",
                     help="fixed tile shape 'terms,order,ctas_per_sm' (implies --no-autotune)")
+    ap.add_argument("--precision", default="mixed", choices=sorted(PRECISIONS),
+                    help="precision of the device-only step (profiling runs; the full run "
+                         "always reports mixed with its FP64 and mixed_a64 legs)")
     args = ap.parse_args()
     if args.tiling:
         args.autotune = False
+    if args.precision != "mixed" and not args.device_only:
+        ap.error("--precision applies to --device-only runs")
     dist = replicas.init("gloo")
     try:
         kind = WORKLOADS[args.workload].get("kind", "cell")
