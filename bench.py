@@ -723,8 +723,10 @@ def run_serve(args, dist):
     srv.close()
     atoms = int(sum(pool[pick[k]].natoms for k in range(nreq)))
     if rank == 0:
-        nb = spec["density"] * 4.0 / 3.0 * np.pi * 6.0 ** 3
-        h2d = atoms / nreq * (48 + 8 * nb)
+        # per request over the bus: positions+element (32 B/atom), lattice and
+        # cell offset up (lists are built on the device); forces, energy and
+        # virial back
+        h2d = atoms / nreq * 32 + 76
         line = {"metric": METRIC, "value": st["atom_steps_per_s"] * dist["world"], "unit": UNIT,
                 "n_gpus": dist["world"], "steps": nreq, "warmup": args.warmup,
                 "ms_per_step": el / nreq * 1e3, "higher_is_better": True, "scaling": "weak",
