@@ -19,6 +19,8 @@
 #ifndef MLIPG_H_
 #define MLIPG_H_
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -276,7 +278,8 @@ void mlipg_server_destroy(mlipg_server* s);
  * cutoff + skin and rebuilt when an atom moves more than skin/2.  Each step
  * runs as one CUDA graph launch when use_graph is non-zero.  Reproduces the
  * trajectories of the reference's regression runs (fix nve,
- * test/regression/*.in); LAMMPS itself owns integration in the drop-in path.
+ * the input scripts in test/regression); LAMMPS itself owns integration in
+ * the drop-in path.
  * mlipg_md_thermo: [pe, ke, T (K), etotal, P, Pxx Pyy Pzz Pxy Pxz Pyz (bar),
  * list rebuilds], with dof = 3N - 3 as LAMMPS's thermo_temp. */
 typedef struct mlipg_md mlipg_md;

@@ -1,0 +1,49 @@
+"""Compile checks of the public C header and of the LAMMPS pair style (CPU).
+
+* include/mlipg.h must compile on its own as C99 and as C++17 with every
+  warning an error: it is what a C, C++ or FFI binding of the library
+  includes.
+* lammps/pair_mlip_gtinv_gpu.cpp is syntax-checked against minimal stand-ins
+  for the LAMMPS declarations it uses (tests/lammps_stub; LAMMPS itself is not
+  part of this repository), with the header's style-registration block too.
+"""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(REPO, "include")
+HEADER = os.path.join(INCLUDE, "mlipg.h")
+STYLE_DIR = os.path.join(REPO, "lammps-mlip-package_gb300", "lammps")
+STUBS = os.path.join(REPO, "tests", "lammps_stub")
+WARN = ["-Wall", "-Wextra", "-Werror"]
+
+
+def run(cmd, stdin=None):
+    p = subprocess.run(cmd, input=stdin, capture_output=True, text=True)
+    assert p.returncode == 0, " ".join(cmd) + "\n" + p.stderr
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="no C compiler")
+def test_header_compiles_as_c99():
+    run(["gcc", "-std=c99", "-pedantic", "-fsyntax-only", *WARN, "-x", "c", HEADER])
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no C++ compiler")
+def test_header_compiles_as_cxx17():
+    run(["g++", "-std=c++17", "-pedantic", "-fsyntax-only", *WARN, "-x", "c++", HEADER])
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no C++ compiler")
+def test_lammps_pair_style_compiles():
+    run(["g++", "-std=c++17", "-fsyntax-only", *WARN, "-I", STUBS, "-I", INCLUDE,
+         os.path.join(STYLE_DIR, "pair_mlip_gtinv_gpu.cpp")])
+    # the registration block LAMMPS's style_pair.h includes
+    src = ('#define PAIR_CLASS\n'
+           '#define PairStyle(key, Class) static const char *style_key = #key;\n'
+           '#include "pair_mlip_gtinv_gpu.h"\n'
+           'const char *registered() { return style_key; }\n')
+    run(["g++", "-std=c++17", "-fsyntax-only", *WARN, "-I", STUBS, "-I", INCLUDE, "-I",
+         STYLE_DIR, "-x", "c++", "-"], stdin=src)
