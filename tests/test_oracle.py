@@ -113,3 +113,36 @@ def test_finite_difference_forces_and_virial(potdir):
         c2.positions = c2.positions @ m
         e.append(o.compute(build_system(c2, o.cutoff, skin=1.0))["energy"])
     assert r["virial"][0] == pytest.approx(-(e[0] - e[1]) / (2 * h), rel=1e-5, abs=1e-4)
+
+
+@pytest.mark.parametrize("maxl, order, gl", [(20, 2, [20]), (16, 3, [16, 6]), (20, 3, [20, 4])])
+def test_high_l_models(tmp_path, maxl, order, gl):
+    """Potentials with l up to 20 (the coupling table's limit): the library
+    builds the model and a schedule for every autotuner tile shape with the
+    coefficient count of the file, and the oracle's forces at l = 20 match
+    finite differences of its energy."""
+    import mlipg
+    from mlipg.potential import gaussian_params, write_potential
+    from mlipg.structures import fcc_cell, jitter
+    path = str(tmp_path / "high_l.mlip")
+    nc = write_potential(path, ["A"], 5.0, gaussian_params(6, 5.0), 1, 1, maxl, order, gl,
+                         [0] * len(gl), masses=[27.0], seed=2)
+    g = mlipg.Potential(path, mlipg.PREC_MIXED)
+    for chunk in (12, 24, 48):
+        for worder in (0, 1, 2):
+            g.set_tiling(chunk, worder, 1)
+    g.close()
+    o = Oracle(path, threads=8)
+    assert o.info["L"] == maxl and o.info["n_coeffs"] == nc
+    rng = np.random.default_rng(3)
+    cell = jitter(fcc_cell(2, 2, 2, 4.05), 0.05, rng)
+    r = o.compute(build_system(cell, o.cutoff, skin=1.0))
+    F = build_system(cell, o.cutoff, skin=1.0).fold_forces(r["f_all"])
+    h = 1e-5
+    for a, k in ((0, 0), (5, 2)):
+        e = []
+        for sgn in (1, -1):
+            c2 = jitter(fcc_cell(2, 2, 2, 4.05), 0.05, np.random.default_rng(3))
+            c2.positions[a, k] += sgn * h
+            e.append(o.compute(build_system(c2, o.cutoff, skin=1.0))["energy"])
+        assert F[a, k] == pytest.approx(-(e[0] - e[1]) / (2 * h), abs=1e-6)
