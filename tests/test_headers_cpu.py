@@ -6,6 +6,8 @@
 * lammps/pair_mlip_gtinv_gpu.cpp is syntax-checked against minimal stand-ins
   for the LAMMPS declarations it uses (tests/lammps_stub; LAMMPS itself is not
   part of this repository), with the header's style-registration block too.
+* the C example of the integration notes (tests/c_api_example.c) compiles,
+  links against the library and runs: a GPU evaluation or MLIPG_ENOGPU.
 """
 import os
 import shutil
@@ -47,3 +49,16 @@ def test_lammps_pair_style_compiles():
            'const char *registered() { return style_key; }\n')
     run(["g++", "-std=c++17", "-fsyntax-only", *WARN, "-I", STUBS, "-I", INCLUDE, "-I",
          STYLE_DIR, "-x", "c++", "-"], stdin=src)
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="no C compiler")
+def test_c_example_links_and_runs(potdir, tmp_path):
+    import mlipg   # builds the library if needed
+    lib = mlipg.lib()._name
+    libdir = os.path.dirname(lib)
+    exe = str(tmp_path / "c_api_example")
+    run(["gcc", "-std=c99", *WARN, "-I", INCLUDE, os.path.join(REPO, "tests", "c_api_example.c"),
+         "-o", exe, "-L", libdir, "-lmlipg", "-Wl,-rpath," + libdir])
+    p = subprocess.run([exe, potdir["gtinv-820"]], capture_output=True, text=True)
+    assert p.returncode == 0, p.stdout + p.stderr
+    assert "elements 2" in p.stdout
