@@ -816,7 +816,13 @@ def run_md(args, dist):
                 "roofline": {"bound": "fp32-cuda-core", "achieved": ach, "peak": peak,
                              "unit": "TFLOP/s", "frac": ach / peak, "traffic": None,
                              "note": "whole MD step time (upper bound of the force kernel)"},
-                "cpu_baseline": None, "clocks": clk, "gpu_launches": None}
+                "cpu_baseline": None, "clocks": clk,
+                # per step one graph of 5 kernels (first half-kick, fused force kernel,
+                # finalize, second half-kick, displacement check); list rebuilds
+                # in the timed region add the device list builder's kernels
+                "gpu_launches": 5 * args.steps,
+                "graph_launches": args.steps,
+                "list_rebuilds": int(th1["rebuilds"] - th0["rebuilds"])}
         print(json.dumps(line), flush=True)
 
 
