@@ -60,6 +60,10 @@ WORKLOADS = {
     # Poisson stream of requests (16..8192 atoms, FP64/mixed 50/50) at 80% of capacity
     "serve-poisson": dict(kind="serve", requests=20000, lo=16, hi=8192, density=0.06,
                           ntypes=2, pot="triclinic-batch", load=0.8, budget=64 << 30),
+    # 256-atom fcc Al at 300 K (run it with --steps 100: 100 NVE steps, dt 1 fs), each
+    # step a CUDA graph
+    "md-fcc-al-256": dict(kind="md", lattice="fcc", n=4, a=4.05, ntypes=1, jitter=0.05,
+                          pot="fcc-al-256", temperature=300.0, dt=0.001),
     # 50 NVE steps of the 1M-atom ternary alloy at 300 K, each step a CUDA graph
     "md-fcc-ternary-1m": dict(kind="md", lattice="fcc", n=64, a=4.0, ntypes=3, jitter=0.1,
                               pot="fcc-ternary-1m", temperature=300.0, dt=0.001),
