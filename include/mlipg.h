@@ -111,7 +111,13 @@ int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double* x, const 
  *   d_fold (optional, NULL): atom -> force row (ghost -> owner).
  *   d_f[nforce*3] accumulated; d_eatom[ncenters] and d_vatom[ncenters][6]
  *   (LAMMPS order) written (optional);
- *   d_out8: [energy, virial xx yy zz xy xz yz, spare] written.
+ *   d_out8: [energy, virial xx yy zz yz zx xy, status] written; d_out8[7]
+ *     holds the launch's status bits as a double (0 = clean; 1: an atom had
+ *     more neighbours inside the cutoff than nb_cap, its energy and forces
+ *     were skipped; 2: an element index outside the potential's elements;
+ *     4: mixed path, adjoint outside the fixed-point range).  The call only
+ *     enqueues work: read d_out8[7] after synchronising the stream, or call
+ *     mlipg_device_status.
  * No counterpart in the reference (its device stages are internal,
  * mlipkk_lmp.h:145-228); this is the entry used by MD loops and batching. */
 int mlipg_compute_device(mlipg_handle* h, int ncenters, const void* d_x4, const int* d_centers,
@@ -129,7 +135,11 @@ int mlipg_compute_device(mlipg_handle* h, int ncenters, const void* d_x4, const 
  * loading the library keeps until exit.  Launches needing more CTA slots
  * fail with MLIPG_ECAPACITY.  All calls share that array: calls that overlap
  * on the GPU race.  The first call on a device resolves the array's device
- * address (cudaGetSymbolAddress); make it before any stream capture.
+ * address (cudaGetSymbolAddress); make it before any stream capture.  The
+ * calling thread's current device must be the handle's (MLIPG_EINVAL
+ * otherwise); the resolved address is kept per device and is stale after a
+ * cudaDeviceReset.  d_out8[7] carries the status bits as for
+ * mlipg_compute_device.
  * No counterpart in the reference. */
 int mlipg_compute_device_noalloc(mlipg_handle* h, int ncenters, const void* d_x4,
                                  const int* d_centers, const int* d_nbr_off,
@@ -140,7 +150,12 @@ int mlipg_compute_device_noalloc(mlipg_handle* h, int ncenters, const void* d_x4
 /* The handle's CUDA stream (cudaStream_t) for ordering caller work. */
 void* mlipg_stream(mlipg_handle* h);
 
-/* Status bits raised by the last kernel run (neighbour capacity, bad element). */
+/* Status bits of the handle's last fused-kernel launch (any entry point):
+ * waits for the handle's stream, then reads the launch's status word
+ * (1 neighbour capacity, 2 element index, 4 mixed-path adjoint range; the
+ * same value as that launch's d_out8[7]).  MD runs, batches and served
+ * requests check the word themselves and fail with MLIPG_ECAPACITY,
+ * MLIPG_EINVAL or MLIPG_ENOTSUP. */
 int mlipg_device_status(mlipg_handle* h, int* bits);
 
 /* Number of regression coefficients / structural features implied by a

@@ -19,6 +19,10 @@
 
 #include "../../include/mlipg.h"
 
+// Maps the fused kernel's status bits (d_out8[7]) to a C-ABI status code and
+// sets the handle's message.
+int mlipg_internal_status_fail(mlipg_handle* h, int bits);
+
 namespace {
 
 __global__ void k_cell_sums(const int* __restrict__ off, const double* __restrict__ eatom,
@@ -77,6 +81,7 @@ struct mlipg_batch {
   Dev<int> centers, d_cell_off;
   Dev<double> f, eatom, vatom, out8, cell7;
   std::vector<double> h_cell7;
+  double h_status = 0;   // d_out8[7] of the last launch: the kernel's status bits
   ~mlipg_batch() {
     // buffers are freed on bs once every evaluation queued on s has finished
     if (done && s && bs && cudaEventRecord(done, s) == cudaSuccess) cudaStreamWaitEvent(bs, done, 0);
@@ -208,8 +213,13 @@ extern "C" int mlipg_batch_results(mlipg_batch* b, double* energies, double* for
     return MLIPG_ECUDA;
   if (cudaMemcpyAsync(b->h_cell7.data(), b->cell7.p, b->h_cell7.size() * sizeof(double),
                       cudaMemcpyDeviceToHost, b->s) != cudaSuccess ||
+      cudaMemcpyAsync(&b->h_status, b->out8.p + 7, sizeof(double), cudaMemcpyDeviceToHost,
+                      b->s) != cudaSuccess ||
       cudaStreamSynchronize(b->s) != cudaSuccess)
     return MLIPG_ECUDA;
+  // a status bit (neighbour capacity, element index, adjoint range) means
+  // some centre's energy and forces are missing: fail the whole batch
+  if (b->h_status != 0.0) return mlipg_internal_status_fail(b->h, (int)b->h_status);
   for (int c = 0; c < b->ncells; ++c) {
     if (energies) energies[c] = b->h_cell7[7 * (size_t)c];
     if (virials)

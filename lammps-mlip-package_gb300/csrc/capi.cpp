@@ -85,10 +85,13 @@ struct mlipg_handle {
   DevBuf d_terms, d_units, d_unit_off, d_nl, d_nl_off, d_poly, d_poly_off, d_wlin, d_radial;
   DevBuf d_terms_f;   // the same terms with the coefficient as FP32 (mixed path)
   DevBuf d_iunits, d_iunit_off, d_tuples, d_wlin_f, d_phase, d_adj_base, d_adj_off, d_adj;
+  DevBuf d_radial_rec;   // FP64 radial recurrence constants (common beta), or empty
+  double rec_q = 0.0;
   // per-call buffers (grow only)
   DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_vatom, d_partials, d_status, d_out8;
   HostBuf h_x4, h_centers, h_off, h_idx, h_f, h_eatom, h_out;
   int last_status = 0;
+  const int* last_status_dev = nullptr;   // status word of the last launch (device)
   int tiling_gen = 0;   // bumped whenever the schedules on the device change
   // per-launch timing of the fused kernel (measurement support)
   bool profiling = false;
@@ -117,6 +120,13 @@ static int cuda_fail(mlipg_handle* h, cudaError_t e, const char* what) {
     cudaError_t e_ = (call);                            \
     if (e_ != cudaSuccess) return cuda_fail(h, e_, what); \
   } while (0)
+
+// FP64 -> FP32 with IEEE overflow to +-inf (a plain cast of a value beyond
+// the FP32 range is undefined in C++)
+static float to_f32(double v) {
+  if (std::fabs(v) > 3.4028234663852886e38) return v > 0 ? INFINITY : -INFINITY;
+  return (float)v;
+}
 
 template <typename T>
 static cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
@@ -174,11 +184,19 @@ static int upload_model(mlipg_handle* h) {
   cudaStream_t s = h->stream;
   CK(upload(h->d_terms, M.cterms, s), "upload terms");
   {
+    // FP32 coefficients for the mixed path, times Y_00^q: its spherical
+    // harmonics are normalised by Y_00 = 1/(2 sqrt(pi)) (exact start of the
+    // FP32 recursion), so an order-q product of its order parameters is
+    // Y_00^-q times the true one
     std::vector<DeviceTerm> tf(M.cterms);
-    for (DeviceTerm& t : tf) {
-      const float cf = (float)t.c;
-      t.c = 0.0;
-      std::memcpy(&t.c, &cf, sizeof cf);   // low word of the 8-byte field
+    const double y00 = 0.28209479177387814347;
+    for (size_t k = 0; k < M.irr_l.size(); ++k) {
+      const double sc = std::pow(y00, (double)M.irr_l[k].size());
+      for (int i = M.irr_cfirst[k]; i < M.irr_cfirst[k] + M.irr_cnterms[k]; ++i) {
+        const float cf = to_f32(tf[i].c * sc);
+        tf[i].c = 0.0;
+        std::memcpy(&tf[i].c, &cf, sizeof cf);   // low word of the 8-byte field
+      }
     }
     CK(upload(h->d_terms_f, tf, s), "upload FP32 terms");
   }
@@ -196,10 +214,37 @@ static int upload_model(mlipg_handle* h) {
   CK(upload(h->d_adj, adj, s), "upload adjoint gather lists");
   CK(upload(h->d_wlin, M.w_lin, s), "upload linear weights");
   {
-    std::vector<float> wf(M.w_lin.begin(), M.w_lin.end());
+    std::vector<float> wf(M.w_lin.size());
+    for (size_t k = 0; k < wf.size(); ++k) wf[k] = to_f32(M.w_lin[k]);
     CK(upload(h->d_wlin_f, wf, s), "upload linear weights (FP32)");
   }
   CK(upload(h->d_radial, radial, s), "upload radial parameters");
+  {
+    // Common beta: f_{n+1} = f_n exp(-beta (mu_{n+1} - mu_n)(mu_{n+1} + mu_n - 2r)),
+    // written with the mean spacing d as exp(2 beta d r) * K_n * exp(eps_n r),
+    // eps_n = 2 beta (mu_{n+1} - mu_n - d); kept when every |eps_n| rc is so
+    // small that exp(eps_n r) = 1 + eps_n r to FP64 precision.
+    const auto& pr = M.pot.params;
+    const int F = (int)pr.size();
+    bool common = F >= 2;
+    for (int n = 1; n < F && common; ++n) common = pr[n].first == pr[0].first;
+    std::vector<double> rec;
+    if (common) {
+      const double beta = pr[0].first;
+      const double d = (pr[F - 1].second - pr[0].second) / (F - 1);
+      for (int n = 0; n + 1 < F; ++n) {
+        const double dn = pr[n + 1].second - pr[n].second;
+        const double eps = 2.0 * beta * (dn - d);
+        if (std::fabs(eps) * M.pot.cutoff > 1e-9) common = false;
+        rec.push_back(std::exp(-beta * dn * (pr[n + 1].second + pr[n].second)));
+        rec.push_back(eps);
+      }
+      h->rec_q = 2.0 * beta * d;
+    }
+    if (!common) rec.clear();
+    CK(upload(h->d_radial_rec, rec, s), "upload radial recurrence");
+    if (rec.empty()) h->d_radial_rec.release();
+  }
   CK(cudaStreamSynchronize(s), "model upload");
   return MLIPG_OK;
 }
@@ -271,7 +316,8 @@ int mlipg_destroy(mlipg_handle* h) {
                     &h->d_iunits, &h->d_iunit_off, &h->d_tuples, &h->d_wlin_f, &h->d_phase,
                     &h->d_terms, &h->d_terms_f, &h->d_units, &h->d_unit_off, &h->d_nl,
                     &h->d_nl_off,
-                    &h->d_poly, &h->d_poly_off, &h->d_wlin, &h->d_radial, &h->d_x4,
+                    &h->d_poly, &h->d_poly_off, &h->d_wlin, &h->d_radial, &h->d_radial_rec,
+                    &h->d_x4,
                     &h->d_centers, &h->d_off, &h->d_idx, &h->d_f, &h->d_eatom, &h->d_vatom, &h->d_partials,
                     &h->d_status, &h->d_out8};
   for (DevBuf* b : bufs) b->release();
@@ -334,34 +380,90 @@ void* mlipg_stream(mlipg_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 int mlipg_device_status(mlipg_handle* h, int* bits) {
   if (!h || !bits) return fail(h, MLIPG_EINVAL, "null argument");
-  *bits = h->last_status;
+  *bits = 0;
+  if (h->device < 0 || !h->last_status_dev) return MLIPG_OK;
+  CK(cudaStreamSynchronize(h->stream), "mlipg_device_status");
+  int v = 0;
+  CK(cudaMemcpy(&v, h->last_status_dev, sizeof(int), cudaMemcpyDeviceToHost), "read status");
+  h->last_status = v;
+  *bits = v;
   return MLIPG_OK;
 }
 
 }  // extern "C"
 
-// Launches the fused kernel and the partial-sum reduction on the handle's stream.
-static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const int* centers,
-                      const int* off, const int* idx, const int* img, const double* cell,
-                      const int* center_cell, const int* fold, int nb_cap, double* f,
-                      double* eatom, double* vatom, double* out8) {
+// Status bits of a launch -> C-ABI status code, with the handle's message.
+static int status_fail(mlipg_handle* h, int bits, int nb_cap) {
+  if (bits & kStatusNeighbourCapacity)
+    return fail(h, MLIPG_ECAPACITY,
+                "an atom has more than %d neighbours inside the cutoff (its energy and "
+                "forces were skipped)",
+                nb_cap);
+  if (bits & kStatusBadType) return fail(h, MLIPG_EINVAL, "element index out of range");
+  if (bits & kStatusAdjointRange)
+    return fail(h, MLIPG_ENOTSUP, "adjoint values outside the mixed path's fixed-point range");
+  return MLIPG_OK;
+}
+
+// Used by the MD, batch and serving layers after reading d_out8[7].
+int mlipg_internal_status_fail(mlipg_handle* h, int bits) {
+  return status_fail(h, bits, 0);
+}
+
+static int effective_nb_cap(int nb_cap) {
+  return std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
+}
+
+// Shared-memory bytes and resident CTAs per SM of the fused kernel for this
+// handle's model, precision and neighbour capacity.
+static int kernel_shape(mlipg_handle* h, int nb_cap, size_t* smem, int* bps) {
   const Model& M = h->model;
   const bool fp64 = h->precision == MLIPG_PREC_FP64;
-  nb_cap = std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
-  const int nl_cap = std::max(M.max_nl, 1);
-  const size_t smem = fused_smem_bytes(fp64, M.T, M.L, nb_cap, nl_cap);
-  if (smem > 227 * 1024)
+  *smem = fused_smem_bytes(fp64, M.T, M.L, nb_cap, std::max(M.max_nl, 1), fp64 ? 0 : M.lh64);
+  if (*smem > 227 * 1024)
     return fail(h, MLIPG_ENOTSUP,
                 "model needs %zu bytes of shared memory per CTA (limit 232448): "
                 "reduce elements, max_l or radial functions",
-                smem);
-  int bps = fused_max_blocks_per_sm(fp64, M.L, smem);
-  if (bps < 1) return fail(h, MLIPG_ENOTSUP, "fused kernel cannot be resident (smem %zu)", smem);
-  if (M.tiling.ctas_per_sm > 0) bps = std::min(bps, M.tiling.ctas_per_sm);
-  int grid = std::max(1, std::min(ncenters, bps * h->num_sms));
-  CK(h->d_partials.reserve((size_t)grid * 8 * sizeof(double)), "alloc partials");
-  CK(h->d_status.reserve(sizeof(int)), "alloc status");
-  CK(cudaMemsetAsync(h->d_status.p, 0, sizeof(int), h->stream), "memset status");
+                *smem);
+  *bps = fused_max_blocks_per_sm(fp64, M.L, *smem);
+  if (*bps < 1) return fail(h, MLIPG_ENOTSUP, "fused kernel cannot be resident (smem %zu)", *smem);
+  if (M.tiling.ctas_per_sm > 0) *bps = std::min(*bps, M.tiling.ctas_per_sm);
+  return MLIPG_OK;
+}
+
+// Grid of the persistent fused kernel for ncenters centres (the number of
+// per-CTA partial-sum slots a launch needs).
+static int launch_grid(mlipg_handle* h, int ncenters, int nb_cap, int* grid) {
+  size_t smem = 0;
+  int bps = 0;
+  const int rc = kernel_shape(h, effective_nb_cap(nb_cap), &smem, &bps);
+  if (rc != MLIPG_OK) return rc;
+  *grid = std::max(1, std::min(ncenters, bps * h->num_sms));
+  return MLIPG_OK;
+}
+
+// Launches the fused kernel and the partial-sum reduction on the handle's
+// stream with the given scratch: per-CTA partial sums (partial_slots rows of
+// 8 doubles) and the status word.  Allocates nothing; with `timed`, brackets
+// the launch with pooled CUDA events (measurement support).
+static int launch_eval(mlipg_handle* h, int ncenters, const double4* x4, const int* centers,
+                       const int* off, const int* idx, const int* img, const double* cell,
+                       const int* center_cell, const int* fold, int nb_cap, double* f,
+                       double* eatom, double* vatom, double* out8, double* partials,
+                       int partial_slots, int* status, bool timed) {
+  const Model& M = h->model;
+  const bool fp64 = h->precision == MLIPG_PREC_FP64;
+  nb_cap = effective_nb_cap(nb_cap);
+  size_t smem = 0;
+  int bps = 0;
+  int rc = kernel_shape(h, nb_cap, &smem, &bps);
+  if (rc != MLIPG_OK) return rc;
+  const int grid = std::max(1, std::min(ncenters, bps * h->num_sms));
+  if (grid > partial_slots)
+    return fail(h, MLIPG_ECAPACITY, "launch needs %d partial-sum slots; the scratch holds %d",
+                grid, partial_slots);
+  CK(cudaMemsetAsync(status, 0, sizeof(int), h->stream), "memset status");
+  h->last_status_dev = status;
   KernelArgs a{};
   a.x4 = x4;
   a.centers = centers;
@@ -373,6 +475,7 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.fold = fold;
   a.ncenters = ncenters;
   a.terms = (fp64 ? h->d_terms : h->d_terms_f).as<DeviceTerm>();
+  a.terms64 = h->d_terms.as<DeviceTerm>();
   a.units = h->d_units.as<DeviceUnit>();
   a.unit_off = h->d_unit_off.as<int>();
   a.iunits = h->d_iunits.as<DeviceIrrUnit>();
@@ -389,23 +492,26 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   a.w_lin_f = h->d_wlin_f.as<float>();
   a.phase_clocks = h->profiling ? h->d_phase.as<unsigned long long>() : nullptr;
   a.radial = h->d_radial.as<double>();
+  a.radial_rec = h->d_radial_rec.as<double>();
+  a.rec_q = h->rec_q;
   a.T = M.T;
   a.F = M.F;
   a.L = M.L;
   a.Lh = M.Lh;
   a.nb_cap = nb_cap;
-  a.nl_cap = nl_cap;
+  a.nl_cap = std::max(M.max_nl, 1);
   a.rc = M.pot.cutoff;
   a.g_bound = (float)M.g_bound;
   a.unit_dyn = M.tiling.warp_order == 2 ? 1 : 0;
   a.sum64 = h->precision == MLIPG_PREC_MIXED_A64 ? 1 : 0;
+  a.lh64 = fp64 ? 0 : M.lh64;
   a.f = f;
   a.eatom = eatom;
   a.vatom = vatom;
-  a.partials = h->d_partials.as<double>();
-  a.status = h->d_status.as<int>();
+  a.partials = partials;
+  a.status = status;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  if (h->profiling && ncenters > 0) {
+  if (timed && h->profiling && ncenters > 0) {
     for (cudaEvent_t* ev : {&ev0, &ev1}) {
       if (!h->ev_pool.empty()) {
         *ev = h->ev_pool.back();
@@ -419,14 +525,30 @@ static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const in
   if (ncenters > 0) {
     CK(launch_fused(fp64, M.L, a, grid, smem, h->stream), "fused kernel launch");
   } else {
-    CK(cudaMemsetAsync(a.partials, 0, 8 * sizeof(double), h->stream), "memset partials");
+    CK(cudaMemsetAsync(partials, 0, 8 * sizeof(double), h->stream), "memset partials");
   }
   if (ev0) {
     CK(cudaEventRecord(ev1, h->stream), "event record");
     h->ev_pending.push_back({ev0, ev1});
   }
-  CK(launch_finalize(a.partials, ncenters > 0 ? grid : 1, out8, h->stream), "finalize launch");
+  CK(launch_finalize(partials, ncenters > 0 ? grid : 1, status, out8, h->stream),
+     "finalize launch");
   return MLIPG_OK;
+}
+
+// The handle's own scratch (grow-only partial sums and status word).
+static int run_kernel(mlipg_handle* h, int ncenters, const double4* x4, const int* centers,
+                      const int* off, const int* idx, const int* img, const double* cell,
+                      const int* center_cell, const int* fold, int nb_cap, double* f,
+                      double* eatom, double* vatom, double* out8) {
+  int grid = 0;
+  const int rc = launch_grid(h, ncenters, nb_cap, &grid);
+  if (rc != MLIPG_OK) return rc;
+  CK(h->d_partials.reserve((size_t)grid * 8 * sizeof(double)), "alloc partials");
+  CK(h->d_status.reserve(sizeof(int)), "alloc status");
+  return launch_eval(h, ncenters, x4, centers, off, idx, img, cell, center_cell, fold, nb_cap, f,
+                     eatom, vatom, out8, h->d_partials.as<double>(), grid,
+                     h->d_status.as<int>(), true);
 }
 
 extern "C" int mlipg_compute_device(mlipg_handle* h, int ncenters, const void* d_x4,
@@ -550,12 +672,7 @@ extern "C" int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double
   int status = 0;
   std::memcpy(&status, h->h_out.as<double>() + 8, sizeof(int));
   h->last_status = status;
-  if (status & kStatusNeighbourCapacity)
-    return fail(h, MLIPG_ECAPACITY, "an atom has more than %d neighbours inside the cutoff",
-                std::max(32, std::min(kNbCapMax, (maxn + 31) / 32 * 32)));
-  if (status & kStatusBadType) return fail(h, MLIPG_EINVAL, "element index out of range");
-  if (status & kStatusAdjointRange)
-    return fail(h, MLIPG_ENOTSUP, "adjoint values outside the mixed path's fixed-point range");
+  if (status) return status_fail(h, status, effective_nb_cap(maxn));
   const double* hf = h->h_f.as<double>();
   const long long nf = (long long)nall * 3;
 #pragma omp parallel for schedule(static)
@@ -723,8 +840,9 @@ extern "C" int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4,
     return fail(h, MLIPG_EINVAL, "mlipg_autotune: invalid arguments");
   const Model& M = h->model;
   const bool fp64 = h->precision == MLIPG_PREC_FP64;
-  const int cap = std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
-  const size_t smem = fused_smem_bytes(fp64, M.T, M.L, cap, std::max(M.max_nl, 1));
+  const int cap = effective_nb_cap(nb_cap);
+  const size_t smem =
+      fused_smem_bytes(fp64, M.T, M.L, cap, std::max(M.max_nl, 1), fp64 ? 0 : M.lh64);
   const int bps_max = std::max(1, fused_max_blocks_per_sm(fp64, M.L, smem));
   // a sample of 16 centres per resident CTA keeps each candidate short
   const int sample = std::min(ncenters, 16 * bps_max * h->num_sms);
@@ -776,11 +894,14 @@ extern "C" int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4,
 }
 
 // Support of the allocation-free entry point (noalloc.cu): the same launch as
-// run_kernel, with the partial-sum and status scratch supplied by the caller
-// and without touching any grow-only buffer (nothing is allocated here).
+// mlipg_compute_device, with the partial-sum and status scratch supplied by
+// the caller and without touching any grow-only buffer (nothing is
+// allocated here; the launch is not bracketed by profiling events).
 int mlipg_internal_fail(mlipg_handle* h, int code, const char* msg) {
   return fail(h, code, "%s", msg);
 }
+
+int mlipg_internal_handle_device(const mlipg_handle* h) { return h ? h->device : -1; }
 
 int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x4,
                                   const int* d_centers, const int* d_nbr_off,
@@ -795,69 +916,7 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
     return fail(h, MLIPG_EINVAL, "mlipg_compute_device_noalloc: invalid arguments");
   if (d_img && (!d_cell || !d_center_cell))
     return fail(h, MLIPG_EINVAL, "image codes need the cell lattices and centre cell ids");
-  const Model& M = h->model;
-  const bool fp64 = h->precision == MLIPG_PREC_FP64;
-  nb_cap = std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
-  const int nl_cap = std::max(M.max_nl, 1);
-  const size_t smem = fused_smem_bytes(fp64, M.T, M.L, nb_cap, nl_cap);
-  if (smem > 227 * 1024)
-    return fail(h, MLIPG_ENOTSUP, "model needs %zu bytes of shared memory per CTA", smem);
-  int bps = fused_max_blocks_per_sm(fp64, M.L, smem);
-  if (bps < 1) return fail(h, MLIPG_ENOTSUP, "fused kernel cannot be resident (smem %zu)", smem);
-  if (M.tiling.ctas_per_sm > 0) bps = std::min(bps, M.tiling.ctas_per_sm);
-  const int grid = std::max(1, std::min(ncenters, bps * h->num_sms));
-  if (grid > partial_slots)
-    return fail(h, MLIPG_ECAPACITY,
-                "launch needs %d partial-sum slots; the no-allocation scratch holds %d", grid,
-                partial_slots);
-  CK(cudaMemsetAsync(status, 0, sizeof(int), h->stream), "memset status");
-  KernelArgs a{};
-  a.x4 = static_cast<const double4*>(d_x4);
-  a.centers = d_centers;
-  a.nbr_off = d_nbr_off;
-  a.nbr_idx = d_nbr_idx;
-  a.img = d_img;
-  a.cell = d_cell;
-  a.center_cell = d_center_cell;
-  a.fold = d_fold;
-  a.ncenters = ncenters;
-  a.terms = (fp64 ? h->d_terms : h->d_terms_f).as<DeviceTerm>();
-  a.units = h->d_units.as<DeviceUnit>();
-  a.unit_off = h->d_unit_off.as<int>();
-  a.iunits = h->d_iunits.as<DeviceIrrUnit>();
-  a.iunit_off = h->d_iunit_off.as<int>();
-  a.tuples = h->d_tuples.as<DeviceTuple>();
-  a.nl_units = h->d_nl.as<DeviceUnit>();
-  a.nl_off = h->d_nl_off.as<int>();
-  a.poly = h->d_poly.as<DevicePoly>();
-  a.poly_off = h->d_poly_off.as<int>();
-  a.adj_base = h->d_adj_base.as<int>();
-  a.adj_off = h->d_adj_off.as<int>();
-  a.adj = h->d_adj.as<DeviceAdj>();
-  a.w_lin = h->d_wlin.as<double>();
-  a.w_lin_f = h->d_wlin_f.as<float>();
-  a.phase_clocks = h->profiling ? h->d_phase.as<unsigned long long>() : nullptr;
-  a.radial = h->d_radial.as<double>();
-  a.T = M.T;
-  a.F = M.F;
-  a.L = M.L;
-  a.Lh = M.Lh;
-  a.nb_cap = nb_cap;
-  a.nl_cap = nl_cap;
-  a.rc = M.pot.cutoff;
-  a.g_bound = (float)M.g_bound;
-  a.unit_dyn = M.tiling.warp_order == 2 ? 1 : 0;
-  a.sum64 = h->precision == MLIPG_PREC_MIXED_A64 ? 1 : 0;
-  a.f = d_f;
-  a.eatom = d_eatom;
-  a.vatom = d_vatom;
-  a.partials = partials;
-  a.status = status;
-  if (ncenters > 0) {
-    CK(launch_fused(fp64, M.L, a, grid, smem, h->stream), "fused kernel launch");
-  } else {
-    CK(cudaMemsetAsync(partials, 0, 8 * sizeof(double), h->stream), "memset partials");
-  }
-  CK(launch_finalize(partials, ncenters > 0 ? grid : 1, d_out8, h->stream), "finalize launch");
-  return MLIPG_OK;
+  return launch_eval(h, ncenters, static_cast<const double4*>(d_x4), d_centers, d_nbr_off,
+                     d_nbr_idx, d_img, d_cell, d_center_cell, d_fold, nb_cap, d_f, d_eatom,
+                     d_vatom, d_out8, partials, partial_slots, status, false);
 }

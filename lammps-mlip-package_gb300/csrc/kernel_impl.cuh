@@ -11,10 +11,14 @@
 //       path: FP32 products summed with Kahan compensation
 //       (mlipkk_lmp.h:314-387, mlipkk_features_kk.h:9-48,
 //       mlipkk_spherical_harmonics_kk.h:18-81)
-//   P3  nonlinear features and polynomial terms of order >= 2: energy part
-//       and H = dE/dd for those features (mlipkk_lmp.h:489-625)
-//   P5  invariants d over the folded coupling table, linear energy
-//       sum w_f d_f, and G = dE/da via H (mlipkk_lmp.h:407-469, 645-733)
+//   P2b mixed path: the order parameters that the polynomial's input
+//       features read, in FP64 (FP64 radial functions, Y_lm and sums)
+//   P3  the polynomial's input features ("nonlinear" features, in FP64) and
+//       their whole energy: linear terms and polynomial terms of order >= 2,
+//       and H = dE/dd for them (mlipkk_lmp.h:489-625)
+//   P5  invariants d over the folded coupling table, the linear energy
+//       sum w_f d_f of the other features, and G = dE/da via H
+//       (mlipkk_lmp.h:407-469, 645-733)
 //   P6  per-pair forces f_ij = sum coeff Re(G . dphi*) with the centre's own
 //       adjoint, scattered as F_i += f, F_j -= f; virial -= r_ij (x) f
 //       (mlipkk_lmp.h:753-922, spherical-harmonic derivatives :117-177)
@@ -56,9 +60,67 @@ __constant__ R cB[kLhMax];
 __constant__ R cLM[kLhMax];        // sqrt((l-m)(l+m+1))
 __constant__ R cDiag[kMaxL + 2];   // -sqrt(1 + 0.5/m), m >= 1
 __constant__ R cOff[kMaxL + 2];    // sqrt(2m + 3)
-__constant__ R cLL[kMaxL + 1];     // sqrt(0.5 l (l+1))
+__constant__ R cLL[kMaxL + 1];     // sqrt(0.5 l (l+1)) (FP32: sqrt(l (l+1)), see sh_visit)
+
+// the same recursion constants in FP64 for the mixed path's FP64 order
+// parameters of the polynomial's input features
+__constant__ double cA64[kLhMax];
+__constant__ double cB64[kLhMax];
+__constant__ double cDiag64[kMaxL + 2];
+__constant__ double cOff64[kMaxL + 2];
 
 __device__ __forceinline__ int lm2i(int l, int m) { return l * (l + 1) / 2 + m; }
+
+// Y_{l,m} (m <= 0, l <= lmax) of one displacement in FP64, by the column
+// recursion of sh_visit below, stored at ys[lmh * stride + slot]
+// (lmh = l(l+1)/2 + l - |m|).
+__device__ __forceinline__ void sh_values64(double dx, double dy, double dz, double r, int lmax,
+                                         double2* ys, int stride, int slot) {
+  const double invr = 1.0 / r;
+  const double ct = dz * invr;
+  const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+  const double rho2 = dx * dx + dy * dy;
+  double cp = 1.0, sp = 0.0;
+  if (rho2 > 0.0) {
+    const double ir = 1.0 / sqrt(rho2);
+    cp = dx * ir;
+    sp = dy * ir;
+  }
+  const double h = 0.70710678118654752440;
+  double pdiag = 0.39894228040143267794;
+  double cm = 1.0, sm = 0.0, cprev = cp, sprev = -sp;
+  const double tc = 2.0 * cp;
+  double sgn = 1.0;
+  for (int mp = 0; mp <= lmax; ++mp) {
+    if (mp > 0) {
+      const double sn = tc * sm - sprev;
+      const double cn = tc * cm - cprev;
+      cprev = cm; cm = cn; sprev = sm; sm = sn;
+      pdiag = pdiag * (cDiag64[mp] * st);
+      sgn = -sgn;
+    }
+    double p1 = 0.0, p2 = 0.0;
+    for (int l = mp; l <= lmax; ++l) {
+      double P;
+      if (l == mp) P = pdiag;
+      else if (l == mp + 1) P = (ct * cOff64[mp]) * p1;
+      else P = cA64[lm2i(l, mp)] * (ct * p1 + cB64[lm2i(l, mp)] * p2);
+      p2 = p1;
+      p1 = P;
+      double yre, yim;
+      if (mp == 0) {
+        yre = P * h;
+        yim = 0.0;
+      } else {
+        const double t = sgn * P * h;
+        yre = t * cm;
+        yim = -(t * sm);
+      }
+      ys[(l * (l + 1) / 2 + l - mp) * stride + slot] = double2{yre, yim};
+    }
+  }
+}
+
 
 __device__ __forceinline__ float rsqrt_r(float v) { return rsqrtf(v); }
 __device__ __forceinline__ double rsqrt_r(double v) { return 1.0 / sqrt(v); }
@@ -71,6 +133,12 @@ __device__ __forceinline__ void sincospi_r(R v, R* s, R* c) { sincospi(v, s, c);
 // associated-Legendre columns are advanced in registers: the recursion of
 // the reference (DLMF 14.10.3 / 14.7.15 with normalised P and Q = P/sin) is
 // the same, evaluated column by column.
+// The FP32 instantiation returns Y / Y_00 (Y_00 = 1/(2 sqrt(pi))): its
+// recursion starts from P = 1, exact, instead of the FP32-rounded
+// normalisation, whose rounding (0.87 ulp) would scale every order parameter
+// alike and bias each order-q invariant by q times that error.  The FP32
+// coupling coefficients carry the factor Y_00^q instead (rounded once per
+// term), and the forces are unchanged: G' dY' = (Y_00 G) (dY / Y_00).
 template <int LCAP, bool DERIV, typename V>
 __device__ __forceinline__ void sh_visit(R dx, R dy, R dz, R r, int L, V& vis) {
   const R invr = R(1) / r;
@@ -83,11 +151,12 @@ __device__ __forceinline__ void sh_visit(R dx, R dy, R dz, R r, int L, V& vis) {
     cp = dx * ir;
     sp = dy * ir;
   }
-  const R h = R(0.70710678118654752440);  // 0.5 * sqrt(2)
+  constexpr bool kUnit = sizeof(R) == 4;   // FP32: Y / Y_00 (see above)
+  const R h = kUnit ? R(1) : R(0.70710678118654752440);  // 0.5 * sqrt(2)
   R Qc[LCAP + 2];
 #pragma unroll
   for (int l = 0; l < LCAP + 2; ++l) Qc[l] = R(0);
-  R pdiag = R(0.39894228040143267794);    // P_0^0 = sqrt(1/(2 pi))
+  R pdiag = kUnit ? R(1) : R(0.39894228040143267794);    // P_0^0 = sqrt(1/(2 pi))
   R cm = R(1), sm = R(0), cprev = cp, sprev = -sp;
   const R tc = R(2) * cp;
   R sgn = R(1);
@@ -104,7 +173,9 @@ __device__ __forceinline__ void sh_visit(R dx, R dy, R dz, R r, int L, V& vis) {
     // next Q column (m = mp + 1): diagonal start
     R qn_diag = R(0);
     if (DERIV) {
-      qn_diag = (mp == 0) ? R(-0.48860251190291992263) : Qc[mp] * (cDiag[mp + 1] * st);
+      // Q_1^1 = P_0^0 cDiag[1]
+      qn_diag = (mp == 0) ? (kUnit ? cDiag[1] : R(-0.48860251190291992263))
+                          : Qc[mp] * (cDiag[mp + 1] * st);
     }
     R p1 = R(0), p2 = R(0), qn1 = R(0), qn2 = R(0);
 #pragma unroll
@@ -264,6 +335,13 @@ struct ESumF {
 };
 __device__ __forceinline__ void eadd(double& e, double v) { e += v; }
 __device__ __forceinline__ void eadd(ESumF& e, float v) { two_sum_acc(e.s, e.c, v); }
+
+// Adds one statically dealt unit's energy to the thread's sum: the mixed
+// path's TwoSum pair, or the FP64 path's double.
+__device__ __forceinline__ void merge_unit_energy(ESumF& es, double&, const ESumF& u) {
+  two_sum_acc(es.s, es.c, u.s);
+}
+__device__ __forceinline__ void merge_unit_energy(ESumF&, double& ed, double u) { ed += u; }
 
 // Sum over the warp's lanes of one unit's energy, identical on every lane.
 // FP64: a butterfly of FP64 adds.  Mixed: a butterfly of TwoSum steps in FP32
@@ -899,15 +977,175 @@ __device__ __forceinline__ void dispatch_unit(const DeviceUnit& u, const DeviceT
   }
 }
 
+// FP64 radial functions f_n(r), n < F (0 for the padding lanes): with a
+// common beta, by the multiplicative recurrence of radial_rec (two exps per
+// neighbour; every step multiplies, so the relative error stays at a few
+// FP64 ulps), else one exp per function.
+__device__ __forceinline__ void radial64(const KernelArgs& A, double r, double* f) {
+  double sn, cs;
+  sincospi(r / A.rc, &sn, &cs);
+  const double fc = r < A.rc ? 0.5 * (cs + 1.0) : 0.0;
+  const int F = A.F;
+  if (A.radial_rec) {
+    const double beta = __ldg(A.radial), mu0 = __ldg(A.radial + 1);
+    const double q = exp(A.rec_q * r);
+    double g = exp(-beta * (r - mu0) * (r - mu0));
+#pragma unroll
+    for (int n = 0; n < kNPad; ++n) {
+      f[n] = n < F ? g * fc : 0.0;
+      if (n + 1 < F) {
+        const double2 ke = __ldg(reinterpret_cast<const double2*>(A.radial_rec) + n);
+        g = g * q * ke.x * fma(ke.y, r, 1.0);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int n = 0; n < kNPad; ++n) {
+      double fv = 0.0;
+      if (n < F) {
+        const double beta = __ldg(A.radial + 2 * n), mu = __ldg(A.radial + 2 * n + 1);
+        const double dr = r - mu;
+        fv = exp(-beta * dr * dr) * fc;
+      }
+      f[n] = fv;
+    }
+  }
+}
+
+// P2b of the mixed path (see fused_kernel): FP64 order parameters
+// a64[element][lmh < lh64][n] of the rows the polynomial's input features
+// read, from FP64 radial functions and Y_lm of the centre's compacted
+// neighbours (misc[t]..misc[t+1] of nbk per element), staged in `stage`
+// (the G space).  With l = 0 alone (model_type 3), a = Y_00 sum_j f_n(r_j):
+// windows of 64 neighbours across elements, one radial evaluation per
+// neighbour and thread.  Not inlined: it runs once per centre and its FP64
+// registers would otherwise weigh on the hot phases.
+__device__ __noinline__ void order_params64(const KernelArgs& A, int c, double4 xi, const int* misc,
+                                            const int* nbk, double2* stage, double2* a64) {
+  const int T = A.T, tid = threadIdx.x;
+  const int lh64 = A.lh64;
+  const int nkeep = misc[T];
+  if (lh64 == 1) {
+    constexpr int kWin = 2 * kChunk;
+    double* fs64 = reinterpret_cast<double*>(stage);   // [kWin][16]
+    const int t = tid >> 4, nn = tid & 15;
+    double acc = 0.0;
+    for (int w0 = 0; w0 < nkeep; w0 += kWin) {
+      const int wsz = min(kWin, nkeep - w0);
+      if (tid < wsz) {
+        const int k = nbk[w0 + tid];
+        const int j = __ldg(A.nbr_idx + k);
+        double dx, dy, dz;
+        pair_disp(A, c, k, xi, A.x4[j], dx, dy, dz);
+        double f64[kNPad];
+        radial64(A, sqrt(dx * dx + dy * dy + dz * dz), f64);
+#pragma unroll
+        for (int q = 0; q < kNPad; ++q) fs64[tid * kNPad + q] = f64[q];
+      }
+      __syncthreads();
+      if (t < T) {
+        const int j0 = max(misc[t], w0), j1 = min(misc[t + 1], w0 + wsz);
+        for (int jj = j0 - w0; jj < j1 - w0; ++jj) acc += fs64[jj * kNPad + nn];
+      }
+      __syncthreads();
+    }
+    // Y_00 = sqrt(1 / (4 pi)), real
+    if (t < T) a64[t * kNPad + nn] = double2{0.28209479177387814347 * acc, 0.0};
+    __syncthreads();
+    return;
+  }
+  int l64 = 0;
+  while ((l64 + 1) * (l64 + 2) / 2 < lh64) ++l64;
+  double2* ys64 = stage;                                                    // [lh64][kChunk]
+  double* fs64 = reinterpret_cast<double*>(ys64 + (size_t)lh64 * kChunk);  // [kChunk][16]
+  const int nent = lh64 * kNPad;
+  // passes of 2 x 256 entries (one pass up to l = 6), two FP64 accumulator
+  // pairs per thread
+  for (int t = 0; t < T; ++t) {
+    for (int e0 = 0; e0 < nent; e0 += 2 * kBlock) {
+      double ar0 = 0.0, ai0 = 0.0, ar1 = 0.0, ai1 = 0.0;
+      const int i0 = e0 + tid, i1 = e0 + kBlock + tid;
+      const int b0 = misc[t], b1 = misc[t + 1];
+      for (int cb = b0; cb < b1; cb += kChunk) {
+        const int csz = min(kChunk, b1 - cb);
+        if (tid < csz) {
+          const int k = nbk[cb + tid];
+          const int j = __ldg(A.nbr_idx + k);
+          double dx, dy, dz;
+          pair_disp(A, c, k, xi, A.x4[j], dx, dy, dz);
+          const double r = sqrt(dx * dx + dy * dy + dz * dz);
+          double f64[kNPad];
+          radial64(A, r, f64);
+#pragma unroll
+          for (int q = 0; q < kNPad; ++q) fs64[tid * kNPad + q] = f64[q];
+          sh_values64(dx, dy, dz, r, l64, ys64, kChunk, tid);
+        }
+        __syncthreads();
+        if (i0 < nent) {
+          const int lmh = i0 >> 4, nn = i0 & 15;
+          for (int jj = 0; jj < csz; ++jj) {
+            const double fv = fs64[jj * kNPad + nn];
+            const double2 y = ys64[lmh * kChunk + jj];
+            ar0 = fma(fv, y.x, ar0);
+            ai0 = fma(-fv, y.y, ai0);
+          }
+        }
+        if (i1 < nent) {
+          const int lmh = i1 >> 4, nn = i1 & 15;
+          for (int jj = 0; jj < csz; ++jj) {
+            const double fv = fs64[jj * kNPad + nn];
+            const double2 y = ys64[lmh * kChunk + jj];
+            ar1 = fma(fv, y.x, ar1);
+            ai1 = fma(-fv, y.y, ai1);
+          }
+        }
+        __syncthreads();
+      }
+      if (i0 < nent) a64[(size_t)t * nent + i0] = double2{ar0, ai0};
+      if (i1 < nent) a64[(size_t)t * nent + i1] = double2{ar1, ai1};
+    }
+  }
+  __syncthreads();
+}
+
+// Invariant d(n) of one (irreps, element tuple) in FP64 from FP64 order
+// parameters a64[element][lmh < lh64][n] (this half-warp's terms; the two
+// halves take alternate terms).  Mixed path, polynomial input features.
+__device__ __forceinline__ double nl_forward64(const DeviceUnit& u,
+                                               const DeviceTerm* __restrict__ terms64,
+                                               const double2* a64, int lh64, int n, int half) {
+  double dsum = 0.0;
+  const int kend = u.term0 + u.nterm;
+  for (int k = u.term0 + half; k < kend; k += 2) {
+    const int4 raw = __ldg(reinterpret_cast<const int4*>(terms64 + k));
+    const double c = __hiloint2double(raw.y, raw.x);
+    const unsigned lw = (unsigned)raw.z, hw = (unsigned)raw.w;
+    const unsigned code = hw >> 16;
+    double pr = 1.0, pi = 0.0;
+    for (int p = 0; p < (int)u.q; ++p) {
+      const int lmh = p < 4 ? (int)((lw >> (8 * p)) & 255u) : (int)((hw >> (8 * (p - 4))) & 255u);
+      const double2 v = a64[((int)u.s[p] * lh64 + lmh) * kNPad + n];
+      const double vi = ((code >> (2 * p)) & 3u) == (unsigned)kSlotConj ? -v.y : v.y;
+      const double tr = pr * v.x - pi * vi;
+      pi = pr * vi + pi * v.x;
+      pr = tr;
+    }
+    const bool self = (code >> 12) & 1u;
+    dsum += (self ? c : 2.0 * c) * pr;
+  }
+  return dsum;
+}
+
 }  // namespace
 
 __host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
 
 struct SmemLayout {
-  size_t a, g, dnl, hnl, nbk, misc, red, total;
+  size_t a, g, dnl, hnl, nbk, misc, red, a64, total;
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int nl_cap) {
+__host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int nl_cap,
+                                                  int lh64) {
   SmemLayout s;
   const size_t an = (size_t)T * Lh * kNPad * sizeof(Rc);
   // adjoint: FP64 re/im, or the mixed path's int32 high + low parts of re/im
@@ -920,7 +1158,8 @@ __host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int
   s.nbk = s.hnl + align16((size_t)nl_cap * kNPad * sizeof(double));
   s.misc = s.nbk + align16((size_t)nb_cap * sizeof(int));
   s.red = s.misc + align16(32 * sizeof(int));
-  s.total = s.red + align16(16 * (kBlock / 32) * sizeof(double));
+  s.a64 = s.red + align16(16 * (kBlock / 32) * sizeof(double));
+  s.total = s.a64 + align16((size_t)T * lh64 * kNPad * sizeof(double2));
   return s;
 }
 
@@ -931,7 +1170,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
   // rows of the a / G arrays per element: the instantiation's capacity, so
   // that element strides are compile-time constants (rows >= Lh are unused)
   constexpr int LS = (LCAP + 1) * (LCAP + 2) / 2;
-  const SmemLayout lay = smem_layout(T, LS, A.nb_cap, A.nl_cap);
+  const SmemLayout lay = smem_layout(T, LS, A.nb_cap, A.nl_cap, sizeof(R) == 4 ? A.lh64 : 0);
   Rc* sa = reinterpret_cast<Rc*>(smem + lay.a);
   R* sg = reinterpret_cast<R*>(smem + lay.g);   // G: Re [T][Lh][16], then Im at sg + gim
   const int gim = T * LS * kNPad;
@@ -1172,22 +1411,50 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       }
     }
     MLIPG_STAMP(1)
-    // ---------------------------------------------------------------- P3
-    double eacc = 0.0;
     const int nl0 = __ldg(A.nl_off + ti), nNL = __ldg(A.nl_off + ti + 1) - nl0;
+    double2* a64 = reinterpret_cast<double2*>(smem + lay.a64);
+    // ---------------------------------------------------------------- P2b
+    // Mixed path: the order parameters that the polynomial's input features
+    // read (l up to the largest l among them), in FP64 from FP64 radial
+    // functions and spherical harmonics.  In fitted potentials the
+    // polynomial's terms are thousands of times larger than the energy they
+    // sum to, so their inputs must carry FP64 accuracy; for model_type 3
+    // these are the l = 0 entries alone.
+    if constexpr (sizeof(R) == 4) {
+      if (A.lh64 > 0 && nNL > 0) {
+        __syncthreads();   // the staging of P2 (same space) is no longer read
+        order_params64(A, c, xi, misc, nbk, reinterpret_cast<double2*>(sg), a64);
+      }
+    }
+    // ---------------------------------------------------------------- P3
+    // The polynomial's input features and their whole energy: linear terms
+    // w_f d_f and the polynomial terms of order >= 2, in FP64.  (The
+    // invariant phase computes no energy for these features, so no large
+    // FP32 partial sums cancel against FP64 ones.)
+    double eacc = 0.0;
     const int n = lane & 15, half = lane >> 4;
     const bool act = n < F;
     if (nNL > 0) {
-      __syncthreads();  // a[] complete
+      __syncthreads();  // a[] (and a64) complete
       for (int u = warp; u < nNL; u += kBlock / 32) {
         const DeviceUnit un = A.nl_units[nl0 + u];
-        R dsum = R(0);
-        GFix gnone{R(1), R(0)};
-        dispatch_unit<false, LS>(un, A.terms, sa, sg, gim, gnone, n, half, act, R(0), dsum);
-        dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
-        if (half == 0) dnl[u * kNPad + n] = act ? (double)dsum : 0.0;
+        double dd;
+        if (sizeof(R) == 4 && A.lh64 > 0) {
+          dd = nl_forward64(un, A.terms64, a64, A.lh64, n, half);
+        } else {
+          R dsum = R(0);
+          GFix gnone{R(1), R(0)};
+          dispatch_unit<false, LS>(un, A.terms, sa, sg, gim, gnone, n, half, act, R(0), dsum);
+          dd = (double)dsum;
+        }
+        dd += __shfl_xor_sync(0xffffffffu, dd, 16);
+        if (half == 0) dnl[u * kNPad + n] = act ? dd : 0.0;
       }
       __syncthreads();
+      for (int e = tid; e < nNL * kNPad; e += kBlock) {
+        const int itc = __ldg(&A.nl_units[nl0 + (e >> 4)].itc);
+        eacc += __ldg(A.w_lin + (size_t)itc * kNPad + (e & 15)) * dnl[e];
+      }
       const int p0 = __ldg(A.poly_off + ti), np = __ldg(A.poly_off + ti + 1) - p0;
 #pragma unroll 4
       for (int pt = tid; pt < np; pt += kBlock) {
@@ -1238,9 +1505,6 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       }
     }
     // ---------------------------------------------------------------- P4
-    // P5 weighs every feature's products with H = w + dE_poly/dd: remove the
-    // nonlinear part's share, sum hnl d over the nonlinear features
-    for (int e = tid; e < nNL * kNPad; e += kBlock) eacc -= hnl[e] * dnl[e];
     // the batched units add hnl to the FP32 weights of every tuple: the mixed
     // path reads an FP32 copy (in the space of dnl, which is no longer read)
     const R* hnlR = reinterpret_cast<const R*>(hnl);
@@ -1318,7 +1582,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           std::conditional_t<sizeof(R) == 4, ESumF, double> eu{};
           run_iu(cur, eu);
           const double e = warp_energy(eu);
-          if (lane == 0) {
+          // units of the polynomial's input features: energy taken in P3
+          if (lane == 0 && !cur.nl) {
             const double sc = e * 0x1p20, hi = rint(sc);
             atomicAdd(efix, (unsigned long long)(long long)hi);
             atomicAdd(efix + 1, (unsigned long long)__double2ll_rn((sc - hi) * 0x1p40));
@@ -1329,8 +1594,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         for (int u = warp; u < nI; u += kBlock / 32) {
           const DeviceIrrUnit iu = A.iunits[i0 + u];
           if (iu.nterm == 0) continue;   // padding of a balanced schedule
-          if constexpr (sizeof(R) == 4) run_iu(iu, esum);
-          else run_iu(iu, eacc);
+          std::conditional_t<sizeof(R) == 4, ESumF, double> eu{};
+          run_iu(iu, eu);
+          // units of the polynomial's input features: energy taken in P3
+          if (!iu.nl) merge_unit_energy(esum, eacc, eu);
         }
       }
       MLIPG_STAMP(3)   // warp 0's batched units (the warps' shares are balanced)
@@ -1345,7 +1612,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         R dsum = R(0);
         dispatch_unit<true, LS>(un, A.terms, sa, sg, gim, gf, n, half, act, (R)hv, dsum);
         dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
-        if (half == 0 && act) eacc += hv * (double)dsum;
+        if (half == 0 && act && un.nl_slot < 0) eacc += hv * (double)dsum;
       }
     }
     if (sizeof(R) != 4) {
@@ -1483,13 +1750,14 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     double s = 0;
     if (tid < 7)
       for (int w = 0; w < kBlock / 32; ++w) s += red[w * 16 + tid];
-    A.partials[(size_t)blockIdx.x * 8 + tid] = s;   // slot 7 is a zeroed spare
+    A.partials[(size_t)blockIdx.x * 8 + tid] = s;   // slot 7 zero (finalize writes the status there)
   }
 }
 
-size_t smem_bytes(int T, int L, int nb_cap, int nl_cap) {
+size_t smem_bytes(int T, int L, int nb_cap, int nl_cap, int lh64) {
   const int lcap = L <= 6 ? 6 : (L <= 12 ? 12 : (L <= 16 ? 16 : 20));   // launch()'s pick
-  return smem_layout(T, (lcap + 1) * (lcap + 2) / 2, nb_cap, nl_cap).total;
+  return smem_layout(T, (lcap + 1) * (lcap + 2) / 2, nb_cap, nl_cap, sizeof(R) == 4 ? lh64 : 0)
+      .total;
 }
 
 template <int LCAP>
@@ -1548,8 +1816,26 @@ cudaError_t init_constants() {
     for (int m = 0; m <= l; ++m) LM[l * (l + 1) / 2 + m] = (R)std::sqrt((double)(l - m) * (l + m + 1));
   for (int m = 1; m <= kMaxL + 1; ++m) dg[m] = (R)(-std::sqrt(1.0 + 0.5 / m));
   for (int m = 0; m <= kMaxL + 1; ++m) of[m] = (R)std::sqrt(2.0 * m + 3.0);
-  for (int l = 0; l <= kMaxL; ++l) ll[l] = (R)std::sqrt(0.5 * l * (l + 1));
+  // the m = 0 derivative factor sqrt(l (l+1)) h; the FP32 instantiation's
+  // harmonics are normalised by Y_00 and carry no factor h = 1/sqrt(2)
+  for (int l = 0; l <= kMaxL; ++l)
+    ll[l] = (R)std::sqrt((sizeof(R) == 4 ? 1.0 : 0.5) * l * (l + 1));
+  double A64[kLhMax] = {}, B64[kLhMax] = {}, dg64[kMaxL + 2] = {}, of64[kMaxL + 2] = {};
+  for (int l = 2; l <= kMaxL; ++l) {
+    const double ls = l * l, lm1s = (l - 1) * (l - 1);
+    for (int m = 0; m <= l - 2; ++m) {
+      const double ms = m * m;
+      A64[l * (l + 1) / 2 + m] = std::sqrt((4.0 * ls - 1.0) / (ls - ms));
+      B64[l * (l + 1) / 2 + m] = -std::sqrt((lm1s - ms) / (4.0 * lm1s - 1.0));
+    }
+  }
+  for (int m = 1; m <= kMaxL + 1; ++m) dg64[m] = -std::sqrt(1.0 + 0.5 / m);
+  for (int m = 0; m <= kMaxL + 1; ++m) of64[m] = std::sqrt(2.0 * m + 3.0);
   cudaError_t e;
+  if ((e = cudaMemcpyToSymbol(cA64, A64, sizeof A64)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(cB64, B64, sizeof B64)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(cDiag64, dg64, sizeof dg64)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(cOff64, of64, sizeof of64)) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(cA, A, sizeof A)) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(cB, B, sizeof B)) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(cLM, LM, sizeof LM)) != cudaSuccess) return e;

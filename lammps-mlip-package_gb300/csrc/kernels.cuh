@@ -31,6 +31,8 @@ struct KernelArgs {
   int ncenters;
   // model (device pointers)
   const DeviceTerm* terms;
+  const DeviceTerm* terms64;  // the table with FP64 coefficients (the mixed path's
+                              // FP64 evaluation of the polynomial's input features)
   const DeviceUnit* units;
   const int* unit_off;    // [T + 1]
   const DeviceIrrUnit* iunits;  // batched-tuple units
@@ -46,11 +48,17 @@ struct KernelArgs {
   const double* w_lin;    // [n_itc][16]
   const float* w_lin_f;   // [n_itc][16], FP32 copy for the mixed path
   const double* radial;   // [F][2] (beta, mu)
+  // Optional recurrence of the FP64 radial functions for a common beta
+  // (null: one exp per function): f_{n+1}/fc = f_n/fc * exp(rec_q r) *
+  // K_n * (1 + eps_n r), radial_rec[n] = (K_n, eps_n)
+  const double* radial_rec;
+  double rec_q;
   int T, F, L, Lh, nb_cap, nl_cap;
   double rc;
   float g_bound;          // mixed path: largest fixed-point adjoint flush (power of two)
   int unit_dyn;           // 1: warps take batched units from a shared counter
   int sum64;              // mixed path: order-parameter sums in plain FP64 FMAs
+  int lh64;               // mixed path: rows of FP64 order parameters (0 = none)
   // outputs
   double* f;              // [nforce][3], accumulated with atomics
   double* eatom;          // [ncenters] (may be null)
@@ -60,11 +68,14 @@ struct KernelArgs {
   unsigned long long* phase_clocks;  // optional [8]: SM cycles spent per phase (P1..P6)
 };
 
-size_t fused_smem_bytes(bool fp64, int T, int L, int nb_cap, int nl_cap);
+size_t fused_smem_bytes(bool fp64, int T, int L, int nb_cap, int nl_cap, int lh64);
 int fused_max_blocks_per_sm(bool fp64, int L, size_t smem);
 cudaError_t launch_fused(bool fp64, int L, const KernelArgs& a, int grid, size_t smem,
                          cudaStream_t s);
-cudaError_t launch_finalize(const double* partials, int nparts, double* out8, cudaStream_t s);
+// Sums the per-CTA partials in a fixed order into out8[0..6] and writes the
+// launch's status bits (as a double) into out8[7].
+cudaError_t launch_finalize(const double* partials, int nparts, const int* status, double* out8,
+                            cudaStream_t s);
 cudaError_t init_device_constants();
 
 }  // namespace mlipg
@@ -72,7 +83,7 @@ cudaError_t init_device_constants();
 namespace mlipg {
 #define MLIPG_DECL_PREC(tag)                                                           \
   namespace tag {                                                                      \
-  size_t smem_bytes(int T, int L, int nb_cap, int nl_cap);                               \
+  size_t smem_bytes(int T, int L, int nb_cap, int nl_cap, int lh64);                     \
   int max_blocks(int L, size_t smem);                                                  \
   cudaError_t launch(int L, const KernelArgs& a, int grid, size_t smem, cudaStream_t s); \
   cudaError_t init_constants();                                                        \

@@ -8,8 +8,9 @@ static_assert(kBlock / 32 == kCtaWarps, "schedules are dealt to the CTA's warps"
 static_assert(sizeof(DeviceUnit) == 32, "DeviceUnit must be 32 bytes");
 static_assert(sizeof(DevicePoly) == 32, "DevicePoly must be 32 bytes");
 
-size_t fused_smem_bytes(bool fp64, int T, int L, int nb_cap, int nl_cap) {
-  return fp64 ? f64::smem_bytes(T, L, nb_cap, nl_cap) : f32::smem_bytes(T, L, nb_cap, nl_cap);
+size_t fused_smem_bytes(bool fp64, int T, int L, int nb_cap, int nl_cap, int lh64) {
+  return fp64 ? f64::smem_bytes(T, L, nb_cap, nl_cap, 0)
+              : f32::smem_bytes(T, L, nb_cap, nl_cap, lh64);
 }
 
 int fused_max_blocks_per_sm(bool fp64, int L, size_t smem) {
@@ -27,8 +28,10 @@ cudaError_t init_device_constants() {
   return f32::init_constants();
 }
 
-// Sums the per-CTA partials [nparts][8] in a fixed order (deterministic).
-__global__ void finalize_kernel(const double* __restrict__ parts, int nparts, double* out) {
+// Sums the per-CTA partials [nparts][8] in a fixed order (deterministic);
+// slot 7 of the output carries the launch's status bits.
+__global__ void finalize_kernel(const double* __restrict__ parts, int nparts,
+                                const int* __restrict__ status, double* out) {
   __shared__ double red[8][33];
   const int q = threadIdx.y;        // 0..7
   const int lane = threadIdx.x;     // 0..31
@@ -39,12 +42,13 @@ __global__ void finalize_kernel(const double* __restrict__ parts, int nparts, do
   if (lane == 0) {
     double t = 0.0;
     for (int k = 0; k < 32; ++k) t += red[q][k];
-    out[q] = t;
+    out[q] = q == 7 ? (double)*status : t;
   }
 }
 
-cudaError_t launch_finalize(const double* partials, int nparts, double* out8, cudaStream_t s) {
-  finalize_kernel<<<1, dim3(32, 8), 0, s>>>(partials, nparts, out8);
+cudaError_t launch_finalize(const double* partials, int nparts, const int* status, double* out8,
+                            cudaStream_t s) {
+  finalize_kernel<<<1, dim3(32, 8), 0, s>>>(partials, nparts, status, out8);
   return cudaGetLastError();
 }
 

@@ -23,6 +23,9 @@
 // Changes whenever the handle's work schedules are rebuilt (autotuning):
 // a captured step holds their device addresses and launch shape.
 int mlipg_internal_tiling_generation(const mlipg_handle* h);
+// Maps the fused kernel's status bits (d_out8[7]) to a C-ABI status code and
+// sets the handle's message.
+int mlipg_internal_status_fail(mlipg_handle* h, int bits);
 
 namespace {
 
@@ -126,7 +129,8 @@ struct mlipg_md {
   cudaGraphExec_t graph = nullptr;
   double graph_dt = 0;
   int graph_tiling = 0;   // schedule generation the graph was captured with
-  int* hflag = nullptr;
+  int* hflag = nullptr;      // pinned: rebuild flag, then (at +8 bytes) the status of the step
+  double* hstat = nullptr;
 };
 
 #define MCK(call)                                                               \
@@ -249,10 +253,11 @@ extern "C" int mlipg_md_create(mlipg_handle* h, const double* lattice9, int nato
       md->out8.alloc(8) != cudaSuccess || md->kin6.alloc(6) != cudaSuccess ||
       md->centers.alloc(natoms) != cudaSuccess || md->flag.alloc(1) != cudaSuccess ||
       mlipg_dnlist_create(md->s, &md->nl) != MLIPG_OK ||
-      cudaHostAlloc(&md->hflag, sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+      cudaHostAlloc(&md->hflag, 16, cudaHostAllocDefault) != cudaSuccess) {
     mlipg_md_destroy(md);
     return MLIPG_ENOMEM;
   }
+  md->hstat = reinterpret_cast<double*>(reinterpret_cast<char*>(md->hflag) + 8);
   cudaMemcpyAsync(md->v.p, vv.data(), vv.size() * sizeof(double), cudaMemcpyHostToDevice, md->s);
   cudaMemcpyAsync(md->minv.p, minv.data(), natoms * sizeof(double), cudaMemcpyHostToDevice, md->s);
   cudaMemcpyAsync(md->m.p, md->mass.data(), natoms * sizeof(double), cudaMemcpyHostToDevice,
@@ -261,7 +266,12 @@ extern "C" int mlipg_md_create(mlipg_handle* h, const double* lattice9, int nato
   cudaMemsetAsync(md->flag.p, 0, sizeof(int), md->s);
   int rc = md_build_list(md, x);
   if (rc == MLIPG_OK) rc = md_forces(md);
-  if (rc == MLIPG_OK && cudaStreamSynchronize(md->s) != cudaSuccess) rc = MLIPG_ECUDA;
+  if (rc == MLIPG_OK &&
+      (cudaMemcpyAsync(md->hstat, md->out8.p + 7, sizeof(double), cudaMemcpyDeviceToHost,
+                       md->s) != cudaSuccess ||
+       cudaStreamSynchronize(md->s) != cudaSuccess))
+    rc = MLIPG_ECUDA;
+  if (rc == MLIPG_OK && *md->hstat != 0.0) rc = mlipg_internal_status_fail(h, (int)*md->hstat);
   if (rc != MLIPG_OK) {
     mlipg_md_destroy(md);
     return rc;
@@ -287,7 +297,12 @@ extern "C" int mlipg_md_run(mlipg_md* md, int nsteps, double dt, int use_graph) 
       MCK(cudaGraphLaunch(md->graph, md->s));
     }
     MCK(cudaMemcpyAsync(md->hflag, md->flag.p, sizeof(int), cudaMemcpyDeviceToHost, md->s));
+    MCK(cudaMemcpyAsync(md->hstat, md->out8.p + 7, sizeof(double), cudaMemcpyDeviceToHost,
+                        md->s));
     MCK(cudaStreamSynchronize(md->s));
+    // the force evaluation of this step raised a status bit (neighbour
+    // capacity, element index, adjoint range): its forces are incomplete
+    if (*md->hstat != 0.0) return mlipg_internal_status_fail(md->h, (int)*md->hstat);
     if (*md->hflag) {
       // an atom moved more than skin/2: rebuild on the device
       rc = md_build_list(md, nullptr);
@@ -346,7 +361,9 @@ extern "C" int mlipg_md_autotune(mlipg_md* md, int max_report, double* report, i
   if (rc != MLIPG_OK) return rc;
   rc = md_forces(md);
   if (rc != MLIPG_OK) return rc;
+  MCK(cudaMemcpyAsync(md->hstat, md->out8.p + 7, sizeof(double), cudaMemcpyDeviceToHost, md->s));
   MCK(cudaStreamSynchronize(md->s));
+  if (*md->hstat != 0.0) return mlipg_internal_status_fail(md->h, (int)*md->hstat);
   return MLIPG_OK;
 }
 

@@ -367,6 +367,7 @@ bool schedules_for_tiling(Model& M, std::string& err) {
     }
   M.sched.assign(T, Schedule());
   M.max_nl = 0;
+  M.lh64 = 0;
   for (int t = 0; t < T; ++t) {
     Schedule& S = M.sched[t];
     std::vector<int> slot(M.n_itc, -1);
@@ -459,6 +460,11 @@ bool schedules_for_tiling(Model& M, std::string& err) {
       return a.nterm > b.nterm;
     });
     M.max_nl = std::max(M.max_nl, (int)S.nl_units.size());
+    for (const DeviceUnit& u : S.nl_units) {
+      const auto& lc = M.irr_l[M.itc[u.itc].irreps];
+      const int lmax = *std::max_element(lc.begin(), lc.end());
+      M.lh64 = std::max(M.lh64, (lmax + 1) * (lmax + 2) / 2);
+    }
     for (size_t pi = 0; pi < M.poly.size(); ++pi) {
       const auto& row = M.poly[pi];
       if (row.size() < 2) continue;
@@ -486,6 +492,23 @@ bool schedules_for_tiling(Model& M, std::string& err) {
       }
     }
     (void)F;
+    // a batched unit is all polynomial inputs or all linear-only features
+    // (nonlinearity is a property of the irreps' order for every model type)
+    for (DeviceIrrUnit& iu : S.iunits) {
+      int nl = -1;
+      const int nt = iu.q == 1 ? T : (iu.q == 2 ? T * T : T * T * T);
+      for (int j = 0; j < nt; ++j) {
+        const DeviceTuple& d = S.tuples[iu.tup + j];
+        if (d.itc < 0) continue;
+        const int v = d.nl_slot >= 0 ? 1 : 0;
+        if (nl >= 0 && nl != v) {
+          err = "internal error: a work unit mixes polynomial and linear-only features";
+          return false;
+        }
+        nl = v;
+      }
+      iu.nl = (uint8_t)(nl > 0 ? 1 : 0);
+    }
     // every feature valid for this element is evaluated exactly once
     std::vector<int> seen(M.n_itc, 0);
     for (const DeviceTuple& d : S.tuples)

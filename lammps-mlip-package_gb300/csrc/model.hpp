@@ -88,7 +88,9 @@ struct DeviceIrrUnit {    // 16 bytes
   int tup;                // first DeviceTuple of this unit's block
   uint8_t q;
   uint8_t s0;             // fixed element of slot 0 (order 4)
-  uint8_t pad[2];
+  uint8_t nl;             // 1: the unit's features are polynomial inputs (their
+                          // energy is taken from the polynomial phase)
+  uint8_t pad;
 };
 struct DeviceTuple {      // 8 bytes
   int itc;                // -1: not a feature (non-canonical ordering)
@@ -146,6 +148,10 @@ struct Model {
   std::vector<Schedule> sched;                // [T]
   Tiling tiling;
   int max_nl = 0;                             // max nonlinear itc over elements
+  // rows (l, m <= 0 entries, l <= the largest l of any nonlinear feature) of
+  // order parameters the mixed path evaluates in FP64 for the polynomial's
+  // input features; 0 when the model has no polynomial terms of order >= 2
+  int lh64 = 0;
   // Largest scaled adjoint flush allowed in the mixed path's fixed-point
   // adjoint accumulation (high parts in multiples of 2^16): a power of two with
   // (flushes per entry) x bound / 2^16 < 2^31, so no integer sum overflows.

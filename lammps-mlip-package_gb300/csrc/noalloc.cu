@@ -22,8 +22,16 @@
 //    overwrites its own slot, so calls that overlap on the GPU (on
 //    different streams, or from different handles) race on it.
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (host code cannot use the symbol itself); make
-//    that first call before any stream capture.
+//    cudaGetSymbolAddress (host code cannot use the symbol itself) and keeps
+//    it for that device; make that first call before any stream capture.
+//    The kept address belongs to the device's current context: after a
+//    cudaDeviceReset it is stale, so reload the library (or restart the
+//    process) before calling again;
+//  * the call runs on the handle's device: the calling thread's current
+//    device must be that device (MLIPG_EINVAL otherwise), so that the
+//    scratch address and the handle's stream belong to the same GPU;
+//  * the launch's status bits are written to d_out8[7] as for
+//    mlipg_compute_device.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -51,6 +59,7 @@ int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x
                                   double* d_f, double* d_eatom, double* d_vatom, double* d_out8,
                                   double* partials, int partial_slots, int* status);
 int mlipg_internal_fail(mlipg_handle* h, int code, const char* msg);
+int mlipg_internal_handle_device(const mlipg_handle* h);
 
 extern "C" int mlipg_compute_device_noalloc(mlipg_handle* h, int ncenters, const void* d_x4,
                                             const int* d_centers, const int* d_nbr_off,
@@ -58,11 +67,18 @@ extern "C" int mlipg_compute_device_noalloc(mlipg_handle* h, int ncenters, const
                                             const double* d_cell, const int* d_center_cell,
                                             const int* d_fold, int nb_cap, double* d_f,
                                             double* d_eatom, double* d_vatom, double* d_out8) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    cudaGetLastError();
+  if (!h) return mlipg_internal_fail(nullptr, MLIPG_EINVAL, "null handle");
+  const int dev = mlipg_internal_handle_device(h);
+  if (dev < 0 || dev >= kMaxDevices)
     return mlipg_internal_fail(h, MLIPG_ENOGPU, "no usable CUDA device for the scratch array");
+  int cur = -1;
+  if (cudaGetDevice(&cur) != cudaSuccess) {
+    cudaGetLastError();
+    return mlipg_internal_fail(h, MLIPG_ENOGPU, "cudaGetDevice failed");
   }
+  if (cur != dev)
+    return mlipg_internal_fail(h, MLIPG_EINVAL,
+                               "the current device differs from the handle's device");
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_mu);

@@ -30,7 +30,9 @@ PairMLIPGtinvGPU::PairMLIPGtinvGPU(LAMMPS *lmp) : Pair(lmp), handle(nullptr)
   one_coeff = 1;
   manybody_flag = 1;
   no_virial_fdotr_compute = 1;    // the library returns the virial
-  precision = MLIPG_PREC_MIXED;
+  // FP64 by default, as the reference pair style (which takes no precision
+  // argument): the drop-in reproduces its energies; `mixed` is opt-in
+  precision = MLIPG_PREC_FP64;
 }
 
 PairMLIPGtinvGPU::~PairMLIPGtinvGPU()

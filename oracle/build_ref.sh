@@ -4,7 +4,8 @@
 # Test infrastructure only; needs the reference sources (REF_SRC) and g++.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF_SRC=${REF_SRC:-/root/reference/src/USER-MLIP}
+# REF_SRC: the reference package's src/USER-MLIP directory (required)
+[ -n "$REF_SRC" ] || { echo "set REF_SRC to the reference's src/USER-MLIP directory" >&2; exit 2; }
 OUT="$HERE/_ref"
 [ -d "$REF_SRC" ] || { echo "reference sources not found: $REF_SRC" >&2; exit 2; }
 mkdir -p "$OUT"

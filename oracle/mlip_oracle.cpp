@@ -910,6 +910,69 @@ int orc_compute(void* h, int nlocal, int nall, const double* x, const int* type,
   return 0;
 }
 
+// Conditioning of the linear energy terms, for the error bound of an
+// evaluation with FP32 products: per owned atom, the sum over the features
+// that enter no polynomial term of order >= 2 ("linear-only" features) of
+// |w_f| * sum_terms |c| prod |a|.  An evaluation whose products and inputs
+// carry a relative error eps errs by at most a small multiple of eps times
+// this sum in those terms.  (The polynomial's input features are not
+// counted: their energy is evaluated in FP64 by the mixed GPU path.)
+// out[nlocal]; 0 for unhandled atoms.  Test infrastructure.
+int orc_linear_conditioning(void* h, int nlocal, int nall, const double* x, const int* type,
+                            const int* off, const int* nbr, double* out) {
+  Oracle* o = static_cast<Oracle*>(h);
+  const Model& M = o->M;
+  const Geometry g{nlocal, nall, x, type, off, nbr};
+  const int F = M.F, La = M.La, ITCn = M.ITC_n;
+  std::vector<char> nl(ITCn, 0);
+  vd w(M.D, 0.0);
+  for (size_t pi = 0; pi < M.poly.size(); ++pi) {
+    if (M.poly[pi].size() >= 2)
+      for (int f : M.poly[pi]) nl[f % ITCn] = 1;
+    else
+      w[M.poly[pi][0]] += M.pot.coeffs[pi];
+  }
+#ifdef _OPENMP
+#pragma omp parallel num_threads(o->nthreads)
+#endif
+  {
+    SHWork sw;
+    vd fn, fnd;
+    AtomState s;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+    for (int i = 0; i < nlocal; ++i) {
+      out[i] = 0.0;
+      const int ti = type[i];
+      if (ti < 0) continue;
+      atom_order_params(M, g, i, s, sw, fn, fnd);
+      double acc = 0.0;
+      for (int f = 0; f < M.D; ++f) {
+        const int itc = f % ITCn;
+        if (nl[itc] || !M.itc[itc].inter[ti] || w[f] == 0.0) continue;
+        const int n = f / ITCn;
+        const auto& tcs = M.itc[itc].type_combs;
+        const int ir = M.itc[itc].irreps;
+        double D = 0.0;
+        for (int term = 0; term < M.irr_nterms[ir]; ++term) {
+          const int it = M.irr_first[ir] + term;
+          double prod = std::fabs(M.term_c[it]);
+          for (size_t p = 0; p < tcs.size(); ++p) {
+            const int t2 = M.other_type[tcs[p]][ti];
+            const cplx v = s.a[((size_t)t2 * F + n) * La + M.term_lm[it][p]];
+            prod *= std::sqrt(v.re * v.re + v.im * v.im);
+          }
+          D += prod;
+        }
+        acc += std::fabs(w[f]) * D;
+      }
+      out[i] = acc;
+    }
+  }
+  return 0;
+}
+
 // Owner-computes evaluation for a list of centre atoms: each centre's energy,
 // and the forces/virial generated by its own adjoint only (the other half of
 // every pair comes from the neighbour's own centre evaluation).  Summed over

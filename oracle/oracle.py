@@ -52,6 +52,8 @@ def lib():
         L.orc_compute.restype = ctypes.c_int
         L.orc_compute.argtypes = [P, ctypes.c_int, ctypes.c_int, dp, ip, ip, ip, dp, dp, dp,
                                   dp, dp]
+        L.orc_linear_conditioning.restype = ctypes.c_int
+        L.orc_linear_conditioning.argtypes = [P, ctypes.c_int, ctypes.c_int, dp, ip, ip, ip, dp]
         L.orc_compute_centers.restype = ctypes.c_int
         L.orc_compute_centers.argtypes = [P, ctypes.c_int, ip, ctypes.c_int, dp, ip, ip, ip,
                                           dp, dp, dp, dp]
@@ -139,6 +141,18 @@ class Oracle:
             i = self.info
             a = an[0::2] + 1j * an[1::2]
             out["anlm"] = a.reshape(sysm.nlocal, i["T"], i["F"], i["Lh"])
+        return out
+
+    def linear_conditioning(self, sysm):
+        """Per owned atom: sum over linear-only features of |w_f| sum_terms |c| prod |a|
+        (the scale of the FP32 rounding error of those energy terms)."""
+        x = np.ascontiguousarray(sysm.x, dtype=np.float64)
+        t = np.ascontiguousarray(sysm.type, dtype=np.int32)
+        off = np.ascontiguousarray(sysm.nbr_off, dtype=np.int32)
+        nb = np.ascontiguousarray(sysm.nbr_idx, dtype=np.int32)
+        out = np.zeros(sysm.nlocal)
+        lib().orc_linear_conditioning(self.h, sysm.nlocal, sysm.nall, _dp(x), _ip(t), _ip(off),
+                                      _ip(nb), _dp(out))
         return out
 
     def compute_centers(self, sysm, centers):

@@ -2,9 +2,12 @@
 
 Each request's result in the mix (many requests in flight, FP64 and mixed
 interleaved) equals the same structure evaluated alone: energies to 1e-13
-relative (they are reduced per cell in a fixed order), forces and virials
-within the precision's repeatability bound (FP64 1e-12, mixed 5e-5 of the
-force / virial scale; the adjoint accumulation uses shared-memory atomics).
+relative (they are reduced per cell in a fixed order), forces and virials to
+1e-12 of the force / virial scale in FP64 (only the order of the FP64 force
+scatter differs) and 1e-8 in the mixed path (its adjoint sums are exact
+fixed point, but the fixed-point scale adapts from the centres a CTA ran
+before, which depend on the batch, and sets the granularity, 2^-37 of the
+largest flush, to which each FP32 flush is rounded; measured 1.2e-9).
 """
 import threading
 
@@ -71,7 +74,7 @@ def test_results_in_the_mix_equal_alone(pot):
         e, f, v = res[k]
         e1, f1, v1 = alone(pot, c, precs[k])
         assert abs(e - e1) <= 1e-13 * abs(e1)
-        tol = 1e-12 if precs[k] == mlipg.PREC_FP64 else 5e-5
+        tol = 1e-12 if precs[k] == mlipg.PREC_FP64 else 1e-8
         assert np.abs(f - f1).max() <= tol * max(np.abs(f1).max(), 1e-30)
         assert np.abs(v - v1).max() <= tol * max(np.abs(v1).max(), 1e-30)
 
