@@ -80,6 +80,13 @@ POT_DESC = {
 }
 SKIN = 1.0
 PRECISIONS = {"mixed": 1, "fp64": 0, "mixed_a64": 2}   # mlipg.PREC_* values
+PRECISION_DESC = ("mixed (MLIPG_PREC_MIXED): FP32 radial functions, Y_lm, invariant and adjoint "
+                  "products; order-parameter neighbour sums in Kahan-compensated FP32 (the "
+                  "mixed_a64 record times the same kernel with plain FP64 sums); the "
+                  "polynomial's input features and their energy, forces, per-atom and total "
+                  "energies and the virial in FP64")
+GOLDEN = os.path.join(REPO, "tests", "golden")
+SOLO = {"rank": 0, "world": 1}   # rank 0's own sub-records (no collectives)
 
 
 def make_cell(spec, n=None, seed=1):
@@ -412,11 +419,14 @@ def run_ours(args, dist):
         fp64_tiling = g.tiling()
     step(nsub)
     torch.cuda.synchronize()
+    clocks64 = ClockSampler(0)
+    clocks64.start()
     ev0.record(stream)
     for _ in range(2):
         step(nsub)
     ev1.record(stream)
     torch.cuda.synchronize()
+    clk64 = clocks64.stop()
     fp64_v = nsub * 2 / (ev0.elapsed_time(ev1) * 1e-3)
     g.set_precision(mlipg.PREC_MIXED)
     g.set_tiling(mixed_tiling["irr_chunk"], mixed_tiling["warp_order"],
@@ -456,6 +466,7 @@ def run_ours(args, dist):
     Fa = small.fold_forces(ra["f_all"])
     acc_a64 = {"force_rms_err_eV_per_A": float(np.sqrt(np.mean((Fa - F64) ** 2))),
                "energy_err_eV_per_atom": abs(ra["energy"] - r64["energy"]) / small.nlocal}
+    acc_fitted = fitted_accuracy() if rank == 0 else None
 
     # ---------------- roofline of the fused kernel
     flops = sum(cnt * g.flops_per_atom_step(t, nb) for t, (cnt, nb) in nbar.items())
@@ -483,8 +494,7 @@ def run_ours(args, dist):
                 "data": "synthetic",
                 "config": {"workload": args.workload, "atoms_per_gpu": natoms,
                            "potential": POT_DESC[spec["pot"]],
-                           "precision": "mixed: FP32 radial/Y_lm/invariant/adjoint products, "
-                                        "FP64 a_nlm sums, forces, energies, virial",
+                           "precision": PRECISION_DESC,
                            "neighbours_in_cutoff_per_atom":
                                {str(k): v[1] for k, v in nbar.items()},
                            "neighbour_list": "full, rc+%.1f A skin, %d pairs (%.0f MB)"
@@ -495,17 +505,63 @@ def run_ours(args, dist):
                            "tiling": tune},
                 "e2e": e2e,
                 "fp64": {"value": fp64_v, "unit": UNIT, "centres": nsub, "tiling": fp64_tiling,
-                         "mixed_over_fp64": value / dist["world"] / fp64_v},
+                         "mixed_over_fp64": value / dist["world"] / fp64_v, "clocks": clk64},
                 "mixed_a64": {"value": a64_v, "unit": UNIT,
                               "what": "MLIPG_PREC_MIXED_A64: order-parameter sums in plain FP64",
                               "accuracy_vs_fp64": acc_a64},
                 "accuracy_mixed_vs_fp64": acc,
+                "accuracy_fitted_potentials": acc_fitted,
                 "energy_eV": e_mixed,
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": 2 * args.steps,
                 "kernel_ms_per_launch": kt, "phase_share": phase_share}
-        print(json.dumps(line), flush=True)
     g.close()
+    if rank == 0 and not args.no_sub_records:
+        # short records of the batched-cell and serving configurations, so that
+        # their rates and latencies are measured in every default run
+        sub = argparse.Namespace(**vars(args))
+        sub.cpu_seconds = 0.0
+        sub.steps, sub.warmup = 3, 1
+        line["batch_4096"] = batch_record(sub, SOLO, "triclinic-batch-4096")
+        sub.requests = 2000
+        line["serving"] = serve_record(sub, SOLO, "serve-poisson")
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def fitted_accuracy():
+    """Mixed (and mixed_a64) against the FP64 path (itself within 1e-10 of the
+    oracle) on the reference's fitted regression potentials and their 32-atom
+    TiAl3 cell: energy error per atom, relative energy error, force RMS error."""
+    import gzip
+    import shutil
+
+    import mlipg
+    from mlipg.structures import read_lammps_data
+    out = {}
+    cell = read_lammps_data(os.path.join(GOLDEN, "structure.lammps"))
+    with tempfile.TemporaryDirectory() as d:
+        for name in ("gtinv-197", "gtinv-820", "gtinv-434"):
+            pot = os.path.join(d, name + ".mlip")
+            with gzip.open(os.path.join(GOLDEN, name + ".mlip.gz"), "rb") as fi, \
+                    open(pot, "wb") as fo:
+                shutil.copyfileobj(fi, fo)
+            g = mlipg.Potential(pot, mlipg.PREC_FP64)
+            s = mlipg.native_system(cell, g.cutoff, 2.0)
+            r64 = g.compute(s)
+            F64 = s.fold_forces(r64["f_all"])
+            rec = {"atoms": s.nlocal, "energy_eV": r64["energy"]}
+            for key, prec in (("mixed", mlipg.PREC_MIXED), ("mixed_a64", mlipg.PREC_MIXED_A64)):
+                g.set_precision(prec)
+                r = g.compute(s)
+                F = s.fold_forces(r["f_all"])
+                rec[key] = {"energy_err_eV_per_atom": abs(r["energy"] - r64["energy"]) / s.nlocal,
+                            "energy_rel_err": abs(r["energy"] - r64["energy"]) /
+                                              abs(r64["energy"]),
+                            "force_rms_err_eV_per_A": float(np.sqrt(np.mean((F - F64) ** 2)))}
+            g.close()
+            out[name] = rec
+    return out
 
 
 # ---------------------------------------------------------------- other configurations
@@ -546,12 +602,18 @@ def type_flops(g, cells_types, nb_mean):
 
 
 def run_batch(args, dist):
+    line = batch_record(args, dist, args.workload)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def batch_record(args, dist, workload):
     """Every cell of the batch evaluated (energy, forces, stress) in one launch."""
     import torch
 
     import mlipg
     from mlipg.potential import workload_potential
-    spec = WORKLOADS[args.workload]
+    spec = WORKLOADS[workload]
     rank = dist["rank"]
     tmp = tempfile.mkdtemp()
     pot = os.path.join(tmp, "pot.mlip")
@@ -637,7 +699,7 @@ def run_batch(args, dist):
                 "n_gpus": dist["world"], "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": el_mixed / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": args.workload, "cells": len(cells), "atoms": natoms,
+                "config": {"workload": workload, "cells": len(cells), "atoms": natoms,
                            "atoms_per_cell": "log-uniform [%d, %d], mean %.1f"
                                              % (spec["lo"], spec["hi"], natoms / len(cells)),
                            "cells_desc": "random triclinic, angles U(60,120) deg, density "
@@ -661,14 +723,21 @@ def run_batch(args, dist):
                         "host_setup_s": create_s[mlipg.PREC_MIXED]},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": 3 * args.steps}
-        print(json.dumps(line), flush=True)
+        return line
+    return None
 
 
 def run_serve(args, dist):
+    line = serve_record(args, dist, args.workload)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def serve_record(args, dist, workload):
     """Poisson request stream against the continuous-batching server."""
     import mlipg
     from mlipg.potential import workload_potential
-    spec = WORKLOADS[args.workload]
+    spec = WORKLOADS[workload]
     rank = dist["rank"]
     tmp = tempfile.mkdtemp()
     pot = os.path.join(tmp, "pot.mlip")
@@ -690,7 +759,8 @@ def run_serve(args, dist):
         return time.perf_counter() - t0
 
     # capacity: a closed burst of requests drawn like the stream
-    srv = mlipg.Server(pot, budget_bytes=spec["budget"], max_batch_atoms=args.max_batch_atoms)
+    srv = mlipg.Server(pot, budget_bytes=spec["budget"], max_batch_atoms=args.max_batch_atoms,
+                       max_batch_atoms_fp64=args.max_batch_atoms_fp64)
     burst(srv, range(min(nreq, 4 * args.warmup)))
     ncap = min(nreq, max(200, nreq // 20))
     tcap = burst(srv, range(ncap))
@@ -701,7 +771,8 @@ def run_serve(args, dist):
     # the stream: exponential inter-arrival gaps at `load` x capacity
     lam = spec["load"] * cap_req
     arrivals = np.cumsum(rng.exponential(1.0 / lam, nreq))
-    srv = mlipg.Server(pot, budget_bytes=spec["budget"], max_batch_atoms=args.max_batch_atoms)
+    srv = mlipg.Server(pot, budget_bytes=spec["budget"], max_batch_atoms=args.max_batch_atoms,
+                       max_batch_atoms_fp64=args.max_batch_atoms_fp64)
     tickets = [None] * nreq
     clocks = ClockSampler(0)
     clocks.start()
@@ -726,6 +797,24 @@ def run_serve(args, dist):
     st = srv.stats()
     srv.close()
     atoms = int(sum(pool[pick[k]].natoms for k in range(nreq)))
+    # roofline: algorithmic FLOPs of every served atom-step (counting rule of
+    # the fused kernel, per element at the pool's mean neighbour count) over
+    # the wall time of the stream, against the FP32 FMA peak; FP64 requests
+    # run on the 64x narrower FP64 pipe, so their FLOPs are also reported apart
+    g = mlipg.Potential(pot, mlipg.PREC_MIXED)
+    nb_mean = 4.18879 * 6.0 ** 3 * spec["density"]
+    fl = np.array([sum(int(np.sum(pool[pick[k]].types == t)) * g.flops_per_atom_step(int(t), nb_mean)
+                       for t in range(spec["ntypes"])) for k in range(nreq)])
+    g.close()
+    peak = mlipg.measure_fma_peak(False)
+    peak64 = mlipg.measure_fma_peak(True)
+    ach = fl.sum() / el / 1e12
+    roof = {"bound": "fp32-cuda-core (mixed requests) / fp64 (FP64 requests)", "achieved": ach,
+            "peak": peak, "unit": "TFLOP/s", "frac": ach / peak, "traffic": None,
+            "fp64_share_of_flops": float(fl[prec == mlipg.PREC_FP64].sum() / fl.sum()),
+            "fp64_peak": peak64,
+            "note": "whole-stream average at %.0f%% offered load (the GPU idles between "
+                    "arrivals)" % (100 * spec["load"])}
     if rank == 0:
         # per request over the bus: positions+element (32 B/atom), lattice and
         # cell offset up (lists are built on the device); forces, energy and
@@ -735,7 +824,7 @@ def run_serve(args, dist):
                 "n_gpus": dist["world"], "steps": nreq, "warmup": args.warmup,
                 "ms_per_step": el / nreq * 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
-                "config": {"workload": args.workload, "requests": nreq,
+                "config": {"workload": workload, "requests": nreq,
                            "atoms_per_request": "log-uniform [%d, %d], mean %.0f"
                                                 % (spec["lo"], spec["hi"], atoms / nreq),
                            "structures": "pool of %d random triclinic cells (density 0.06/A^3,"
@@ -745,6 +834,8 @@ def run_serve(args, dist):
                            "potential": POT_DESC[spec["pot"]],
                            "budget_bytes": spec["budget"],
                            "max_batch_atoms": args.max_batch_atoms,
+                           "max_batch_atoms_fp64": args.max_batch_atoms_fp64 or
+                                                   min(8192, args.max_batch_atoms),
                            "offered_load": spec["load"],
                            "step": "one request (energy + forces + stress)"},
                 "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"]},
@@ -755,9 +846,10 @@ def run_serve(args, dist):
                         "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(24 * atoms / nreq + 56),
                         "api": "mlipg_server_submit / mlipg_server_wait with host arrays"},
-                "roofline": None, "cpu_baseline": cpu, "clocks": clk,
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": int(3 * st["batches"])}
-        print(json.dumps(line), flush=True)
+        return line
+    return None
 
 
 def run_md(args, dist):
@@ -838,7 +930,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fcc-ternary-1m", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--fp64-fraction", type=float, default=1.0 / 32)
+    ap.add_argument("--fp64-fraction", type=float, default=1.0 / 8)
     ap.add_argument("--centres", type=int, default=0,
                     help="evaluate only the first N centres per step (profiling runs)")
     ap.add_argument("--device-only", action="store_true",
@@ -848,6 +940,10 @@ def main():
     ap.add_argument("--pool", type=int, default=256,
                     help="serving: distinct structures the requests are drawn from")
     ap.add_argument("--max-batch-atoms", type=int, default=65536)
+    ap.add_argument("--max-batch-atoms-fp64", type=int, default=0,
+                    help="serving: FP64 batch cap (0: the server's default)")
+    ap.add_argument("--no-sub-records", action="store_true",
+                    help="skip the short batch and serving records of the default run")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default tile shape instead of autotuning it")
     ap.add_argument("--tiling", default="",

@@ -45,8 +45,12 @@ enum mlipg_precision {
   MLIPG_PREC_MIXED = 1,     /* FP32 radial/Y_lm/invariant/adjoint products;
                                order-parameter neighbour sums (Kahan) and unit
                                energies (TwoSum) in compensated FP32, at FP32
-                               pipe speed; force, per-atom and total energy
-                               and virial accumulation in FP64 */
+                               pipe speed; the polynomial's input features
+                               and their energy in FP64 (FP64 order
+                               parameters); force, per-atom and total energy
+                               and virial accumulation in FP64.  Energy error:
+                               a few FP32 ulps of sum |w_f| |d_f| over the
+                               other (linear-only) features */
   MLIPG_PREC_MIXED_A64 = 2  /* as MLIPG_PREC_MIXED, with the order-parameter
                                neighbour sums made with plain FP64 FMAs */
 };
@@ -269,8 +273,12 @@ int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4, const int* d
  * size, evaluated by continuous batching.  Requests (mlipg_server_submit,
  * thread-safe) are admitted in arrival order against a device-memory budget,
  * grouped by precision (MLIPG_PREC_FP64 or MLIPG_PREC_MIXED; other values are
- * MLIPG_EINVAL) into batches of at most max_batch_atoms atoms and launched as
- * they arrive; FP64 and mixed batches run on separate streams.
+ * MLIPG_EINVAL) into batches of at most max_batch_atoms atoms (FP64 batches:
+ * at most min(max_batch_atoms, 8192) unless set by
+ * mlipg_server_set_batch_atoms) and launched as they arrive; a precision
+ * whose batch is full stops taking requests while the other precision is
+ * still admitted in arrival order; FP64 and mixed batches run on separate
+ * streams.
  * mlipg_server_wait returns a request's energy, forces[natoms*3] and virial
  * (LAMMPS order) or MLIPG_ETIMEDOUT at its deadline.  A request's energy
  * does not depend on the other requests in its batch.
@@ -279,6 +287,7 @@ int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4, const int* d
 typedef struct mlipg_server mlipg_server;
 int mlipg_server_create(const char* potential_path, size_t device_budget_bytes,
                         int max_batch_atoms, mlipg_server** out);
+int mlipg_server_set_batch_atoms(mlipg_server* s, int precision, int max_atoms);
 int mlipg_server_submit(mlipg_server* s, int natoms, const double* lattice9, const double* x,
                         const int* elements, int precision, long long* ticket);
 int mlipg_server_wait(mlipg_server* s, long long ticket, int timeout_ms, double* energy,

@@ -4,7 +4,11 @@
 // Requests are queued by mlipg_server_submit (any thread).  One worker
 // thread admits queued requests in arrival order while their estimated
 // device footprint fits the memory budget, groups them by precision into
-// batches of at most `max_batch_atoms` atoms, builds the image-coded
+// batches of at most `max_batch_atoms` atoms (a separate, smaller cap for
+// FP64 batches: an FP64 evaluation costs some twenty times a mixed one of
+// the same size, and one long FP64 batch would hold every request queued
+// behind it; a precision whose batch is full stops taking requests while
+// the other one keeps being admitted in arrival order), builds the image-coded
 // neighbour lists and launches each batch (one persistent launch over all
 // its cells) on the stream of that precision's handle.  Batches stay
 // resident on the device (positions, lists, outputs) until their results
@@ -59,6 +63,9 @@ struct InFlight {
   size_t bytes = 0;
 };
 
+// default cap of FP64 batches (atoms); mlipg_server_set_batch_atoms changes it
+constexpr int kDefaultFp64BatchAtoms = 8192;
+
 size_t estimate_bytes(int natoms, double cutoff) {
   // positions/forces/energies/virials per atom + ~density * sphere neighbours
   const double nbar = 0.1 * 4.18879 * cutoff * cutoff * cutoff;   // generous density 0.1/A^3
@@ -70,7 +77,7 @@ size_t estimate_bytes(int natoms, double cutoff) {
 struct mlipg_server {
   mlipg_handle* h[2] = {nullptr, nullptr};   // FP64, mixed
   size_t budget = 0;
-  int max_batch_atoms = 0;
+  int max_batch_atoms[2] = {0, 0};            // FP64, mixed
   double cutoff = 0;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -132,18 +139,30 @@ static void worker_loop(mlipg_server* s) {
         s->cv_work.wait_for(lock, std::chrono::milliseconds(2));
         continue;
       }
+      // arrival order; the budget is shared (a request that does not fit stops
+      // all admission, an oversized one runs alone), the batch caps are per
+      // precision (a full batch closes its precision only)
       int atoms[2] = {0, 0};
-      while (!s->queue.empty()) {
-        auto& r = s->queue.front();
+      bool closed[2] = {false, false};
+      for (auto it = s->queue.begin(); it != s->queue.end() && !(closed[0] && closed[1]);) {
+        auto& r = *it;
         const int p = r->precision == MLIPG_PREC_FP64 ? 0 : 1;
+        if (closed[p]) {
+          ++it;
+          continue;
+        }
         const bool fits = s->used + take_bytes[0] + take_bytes[1] + r->est_bytes <= s->budget;
         const bool alone = s->inflight.empty() && take[0].empty() && take[1].empty();
         if (!fits && !alone) break;   // wait for memory; an oversized request runs alone
-        if (!take[p].empty() && atoms[p] + r->natoms > s->max_batch_atoms) break;
+        if (!take[p].empty() && atoms[p] + r->natoms > s->max_batch_atoms[p]) {
+          closed[p] = true;
+          ++it;
+          continue;
+        }
         atoms[p] += r->natoms;
         take_bytes[p] += r->est_bytes;
         take[p].push_back(r);
-        s->queue.pop_front();
+        it = s->queue.erase(it);
       }
       s->used += take_bytes[0] + take_bytes[1];
     }
@@ -229,10 +248,19 @@ extern "C" int mlipg_server_create(const char* potential_path, size_t device_bud
     }
   }
   s->budget = device_budget_bytes;
-  s->max_batch_atoms = max_batch_atoms;
+  s->max_batch_atoms[1] = max_batch_atoms;
+  s->max_batch_atoms[0] = std::min(max_batch_atoms, kDefaultFp64BatchAtoms);
   s->cutoff = mlipg_cutoff(s->h[0]);
   s->worker = std::thread(worker_loop, s);
   *out = s;
+  return MLIPG_OK;
+}
+
+extern "C" int mlipg_server_set_batch_atoms(mlipg_server* s, int precision, int max_atoms) {
+  if (!s || max_atoms <= 0 || (precision != MLIPG_PREC_FP64 && precision != MLIPG_PREC_MIXED))
+    return MLIPG_EINVAL;
+  std::lock_guard<std::mutex> lock(s->mu);
+  s->max_batch_atoms[precision == MLIPG_PREC_FP64 ? 0 : 1] = max_atoms;
   return MLIPG_OK;
 }
 

@@ -85,6 +85,7 @@ def lib():
         "mlipg_batch_results": (i32, [P, dp, dp, dp]),
         "mlipg_batch_device_bytes": (ctypes.c_size_t, [P]),
         "mlipg_server_create": (i32, [ctypes.c_char_p, ctypes.c_size_t, i32, ctypes.POINTER(P)]),
+        "mlipg_server_set_batch_atoms": (i32, [P, i32, i32]),
         "mlipg_server_submit": (i32, [P, i32, dp, dp, ip, i32, llp]),
         "mlipg_server_wait": (i32, [P, ctypes.c_longlong, i32, dp, dp, dp]),
         "mlipg_server_stats": (i32, [P, dp]),
@@ -456,13 +457,16 @@ class Server:
     STATS = ["completed", "p50_ms", "p99_ms", "atom_steps_per_s", "batches", "device_bytes",
              "queued", "in_flight"]
 
-    def __init__(self, path: str, budget_bytes: int = 64 << 30, max_batch_atoms: int = 65536):
+    def __init__(self, path: str, budget_bytes: int = 64 << 30, max_batch_atoms: int = 65536,
+                 max_batch_atoms_fp64: int = 0):
         lib()
         h = ctypes.c_void_p()
         _check(lib().mlipg_server_create(os.fsencode(path), budget_bytes, max_batch_atoms,
                                          ctypes.byref(h)))
         self.h = h
         self.natoms = {}
+        if max_batch_atoms_fp64 > 0:
+            _check(lib().mlipg_server_set_batch_atoms(self.h, PREC_FP64, max_batch_atoms_fp64))
 
     def submit(self, cell, precision: int) -> int:
         lat = np.ascontiguousarray(cell.lattice, dtype=np.float64)

@@ -4,10 +4,12 @@ Each request's result in the mix (many requests in flight, FP64 and mixed
 interleaved) equals the same structure evaluated alone: energies to 1e-13
 relative (they are reduced per cell in a fixed order), forces and virials to
 1e-12 of the force / virial scale in FP64 (only the order of the FP64 force
-scatter differs) and 1e-8 in the mixed path (its adjoint sums are exact
+scatter differs) and 1e-7 in the mixed path: its adjoint sums are exact
 fixed point, but the fixed-point scale adapts from the centres a CTA ran
-before, which depend on the batch, and sets the granularity, 2^-37 of the
-largest flush, to which each FP32 flush is rounded; measured 1.2e-9).
+before, which depend on the batch, and each FP32 flush is rounded to
+2^-31 .. 2^-37 of the CTA's largest flush (measured differences up to 1.2e-8
+of the force scale, below the 6e-8 rounding of the FP32 products
+themselves).
 """
 import threading
 
@@ -74,7 +76,7 @@ def test_results_in_the_mix_equal_alone(pot):
         e, f, v = res[k]
         e1, f1, v1 = alone(pot, c, precs[k])
         assert abs(e - e1) <= 1e-13 * abs(e1)
-        tol = 1e-12 if precs[k] == mlipg.PREC_FP64 else 1e-8
+        tol = 1e-12 if precs[k] == mlipg.PREC_FP64 else 1e-7
         assert np.abs(f - f1).max() <= tol * max(np.abs(f1).max(), 1e-30)
         assert np.abs(v - v1).max() <= tol * max(np.abs(v1).max(), 1e-30)
 
