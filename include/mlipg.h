@@ -317,6 +317,29 @@ int mlipg_md_thermo(mlipg_md* md, double* out12);
 int mlipg_md_autotune(mlipg_md* md, int max_report, double* report, int* nreport);
 void mlipg_md_destroy(mlipg_md* md);
 
+/* Training features of one periodic cell, the quantities a potential is
+ * fitted to: its energy, forces and stress are linear in the regression
+ * coefficients w (in the order of the potential file),
+ *   E = sum_i polynomial[i] . w,  F_k = force[k] . w,  stress = stress . w.
+ * Outputs (any may be NULL; host arrays):
+ *   structural [natoms][n_structural]: the invariants d_{i,f}, feature index
+ *     f = n * n_itc + itc as in the reference;
+ *   polynomial [natoms][n_polynomial]: P_{i,p} = prod_{f in p} d_{i,f};
+ *   force [natoms][n_polynomial][3]: the forces of E_p = sum_i P_{i,p}
+ *     (F = force . w);
+ *   stress [n_polynomial][6]: -sum over pairs r_ij (x) dE_p/dr_ij, order
+ *     xx yy zz yz zx xy as the reference's stress features.
+ * lattice9: cell vectors a1 a2 a3 as rows; x[natoms*3]; elements 0-based.
+ * Evaluated in FP64 on the device (neighbour list built there).
+ * Replaces MLIPModel::set_structure + prepare_features and the getters
+ * get_structural_features / get_polynomial_features / get_force_features /
+ * get_stress_features (src/USER-MLIP/mlipkk.cpp:278-372, 461-470, 992-1281,
+ * 1322-1381).  mlipg_feature_sizes gives n_structural and n_polynomial. */
+int mlipg_feature_sizes(const mlipg_handle* h, long long* n_structural, long long* n_polynomial);
+int mlipg_features(mlipg_handle* h, int natoms, const double* lattice9, const double* x,
+                   const int* elements, double* structural, double* polynomial, double* force,
+                   double* stress);
+
 /* Host neighbour-list builder for standalone and batched use: owned atoms
  * (wrapped into the cell), ghost images within `cutoff` in fractional
  * coordinates (LAMMPS's ghost rule for triclinic boxes), each atom's owner

@@ -22,6 +22,9 @@
 
 using namespace mlipg;
 
+struct mlipg_handle;
+void mlipg_internal_features_release(const mlipg_handle* h);   // features.cu
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -312,6 +315,7 @@ int mlipg_destroy(mlipg_handle* h) {
     delete h;
     return MLIPG_OK;
   }
+  mlipg_internal_features_release(h);
   DevBuf* bufs[] = {&h->d_adj_base, &h->d_adj_off, &h->d_adj,
                     &h->d_iunits, &h->d_iunit_off, &h->d_tuples, &h->d_wlin_f, &h->d_phase,
                     &h->d_terms, &h->d_terms_f, &h->d_units, &h->d_unit_off, &h->d_nl,
@@ -902,6 +906,8 @@ int mlipg_internal_fail(mlipg_handle* h, int code, const char* msg) {
 }
 
 int mlipg_internal_handle_device(const mlipg_handle* h) { return h ? h->device : -1; }
+const Model* mlipg_internal_model(const mlipg_handle* h) { return h ? &h->model : nullptr; }
+int mlipg_internal_num_sms(const mlipg_handle* h) { return h ? std::max(h->num_sms, 1) : 1; }
 
 int mlipg_internal_launch_scratch(mlipg_handle* h, int ncenters, const void* d_x4,
                                   const int* d_centers, const int* d_nbr_off,

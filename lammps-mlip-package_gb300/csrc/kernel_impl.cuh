@@ -26,7 +26,9 @@
 // neighbour's own evaluation (identical to the reference's j<i / ghost
 // split up to summation order).
 //
-// Required macros: MLIPG_REAL (float|double), MLIPG_TAG (f32|f64).
+// Required macros: MLIPG_REAL (float|double), MLIPG_TAG (f32|f64); with
+// MLIPG_NO_FUSED defined, only the device helpers (spherical harmonics,
+// radial basis, displacements) and init_constants are compiled.
 
 #include <cuda_runtime.h>
 
@@ -1163,6 +1165,7 @@ __host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int
   return s;
 }
 
+#ifndef MLIPG_NO_FUSED   // units that only want the device helpers above
 template <int LCAP>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_constant__ KernelArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1800,6 +1803,8 @@ cudaError_t launch(int L, const KernelArgs& a, int grid, size_t smem, cudaStream
   }
   return cudaGetLastError();
 }
+
+#endif  // MLIPG_NO_FUSED
 
 cudaError_t init_constants() {
   R A[kLhMax] = {}, B[kLhMax] = {}, LM[kLhMax] = {}, dg[kMaxL + 2] = {}, of[kMaxL + 2] = {},

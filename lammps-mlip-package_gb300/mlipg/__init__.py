@@ -96,6 +96,8 @@ def lib():
         "mlipg_autotune": (i32, [P, i32, P, P, P, P, P, P, P, i32, P, P, i32, dp, ip]),
         "mlipg_batch_autotune": (i32, [P, i32, dp, ip]),
         "mlipg_md_autotune": (i32, [P, i32, dp, ip]),
+        "mlipg_feature_sizes": (i32, [P, llp, llp]),
+        "mlipg_features": (i32, [P, i32, dp, dp, ip, dp, dp, dp, dp]),
         "mlipg_dnlist_create": (i32, [P, ctypes.POINTER(P)]),
         "mlipg_dnlist_build": (i32, [P, i32, ip, dp, P, ctypes.c_double, i32]),
         "mlipg_dnlist_arrays": (i32, [P, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P),
@@ -295,6 +297,26 @@ class Potential:
         _check(lib().mlipg_compute_device(self.h, ncenters, x4, centers, nbr_off, nbr_idx,
                                           img, cell, center_cell, fold, nb_cap, f, eatom, vatom,
                                           out8), self.h)
+
+    def features(self, cell, want=("d", "p", "ff", "sf")):
+        """Training features of a periodic cell (see mlipg_features): structural d
+        [natoms, D], polynomial p [natoms, C], force ff [natoms, C, 3] and stress
+        sf [C, 6] (order xx yy zz yz zx xy), with E = p.sum(0) . w, F = ff . w and
+        the virial sf . w for the coefficients w."""
+        nd, nc = ctypes.c_longlong(), ctypes.c_longlong()
+        _check(lib().mlipg_feature_sizes(self.h, ctypes.byref(nd), ctypes.byref(nc)), self.h)
+        D, C, n = nd.value, nc.value, cell.natoms
+        out = {"d": np.zeros((n, D)) if "d" in want else None,
+               "p": np.zeros((n, C)) if "p" in want else None,
+               "ff": np.zeros((n, C, 3)) if "ff" in want else None,
+               "sf": np.zeros((C, 6)) if "sf" in want else None}
+        lat = np.ascontiguousarray(cell.lattice, dtype=np.float64)
+        x = np.ascontiguousarray(cell.positions, dtype=np.float64)
+        t = np.ascontiguousarray(cell.types, dtype=np.int32)
+        _check(lib().mlipg_features(self.h, n, _dp(lat), _dp(x), _ip(t),
+                                    *[(_dp(out[k]) if out[k] is not None else None)
+                                      for k in ("d", "p", "ff", "sf")]), self.h)
+        return {k: v for k, v in out.items() if v is not None}
 
     def set_profiling(self, on: bool):
         _check(lib().mlipg_set_profiling(self.h, 1 if on else 0), self.h)

@@ -737,6 +737,12 @@ void orc_info(void* h, int* out13, double* cutoff) {
   *cutoff = M.pot.cutoff;
 }
 
+// regression coefficients (divided by their scales), [n_coeffs]
+void orc_coeffs(void* h, double* out) {
+  const Model& M = static_cast<Oracle*>(h)->M;
+  std::copy(M.pot.coeffs.begin(), M.pot.coeffs.end(), out);
+}
+
 // flattened model structure for cross-checks: itc list and polynomial index
 // itc_out: for each itc [irreps, q, tc_0..tc_{q-1}] concatenated; returns total ints
 long orc_dump_itc(void* h, int* out, long cap) {
@@ -907,6 +913,177 @@ int orc_compute(void* h, int nlocal, int nall, const double* x, const int* type,
   // LAMMPS order xx yy zz xy xz yz, mlipkk_lmp.h:942-955
   virial[0] = sxx; virial[1] = syy; virial[2] = szz;
   virial[3] = sxy; virial[4] = szx; virial[5] = syz;
+  return 0;
+}
+
+// Training features of one structure (the reference's prepare_features:
+// mlipkk.cpp:461-470 with compute_structural_features :609-666,
+// compute_polynomial_features :1167-1179, compute_dirj :1011-1154 and
+// compute_force_and_stress_features :1181-1281), on a full neighbour list
+// with ghost atoms in the owner-computes form: centre i's features d_i,
+// its polynomial features P_i,p = prod_{f in p} d_i,f, and for every
+// neighbour j the derivative of d_i with respect to the pair displacement
+// r_j - r_i (the reference's dirj), contracted into the force features
+// FF[i][p] += dP_i,p/dr_ij, FF[j][p] -= dP_i,p/dr_ij and the stress features
+// SF[p] -= r_ij (x) dP_i,p/dr_ij (reference order xx yy zz yz zx xy).
+// Summed over all centres this is the reference's half-list result, and
+// E = sum_i P_i . w, F = FF . w, virial = SF . w for the coefficients w.
+// d_out [nlocal][D], p_out [nlocal][C], ff_out [nall][C][3] (accumulated),
+// sf_out [C][6] (accumulated); any may be null.  Test infrastructure.
+int orc_features(void* h, int nlocal, int nall, const double* x, const int* type, const int* off,
+                 const int* nbr, double* d_out, double* p_out, double* ff_out, double* sf_out) {
+  Oracle* o = static_cast<Oracle*>(h);
+  const Model& M = o->M;
+  const Geometry g{nlocal, nall, x, type, off, nbr};
+  const int F = M.F, La = M.La, ITCn = M.ITC_n, D = M.D;
+  const int C = (int)M.poly.size();
+  int nth = o->nthreads;
+  std::vector<vd> ffb(nth), sfb(nth);
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nth)
+#endif
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    vd& ffl = ffb[tid];
+    vd& sfl = sfb[tid];
+    if (ff_out) ffl.assign((size_t)nall * C * 3, 0.0);
+    if (sf_out) sfl.assign((size_t)C * 6, 0.0);
+    SHWork w;
+    vd fn, fnd;
+    AtomState s;
+    vd dirj((size_t)D * 3);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+    for (int i = 0; i < nlocal; ++i) {
+      const int ti = type[i];
+      if (ti < 0) continue;
+      atom_order_params(M, g, i, s, w, fn, fnd);
+      // structural features, mlipkk.cpp:628-663
+      vd d(D, 0.0);
+      for (int f = 0; f < D; ++f) {
+        const int itc = f % ITCn;
+        if (!M.itc[itc].inter[ti]) continue;
+        const int n = f / ITCn;
+        const auto& tcs = M.itc[itc].type_combs;
+        const int ir = M.itc[itc].irreps;
+        double feat = 0.0;
+        for (int term = 0; term < M.irr_nterms[ir]; ++term) {
+          const int it = M.irr_first[ir] + term;
+          cplx tmp = {M.term_c[it], 0.0};
+          for (size_t p = 0; p < tcs.size(); ++p) {
+            const int t2 = M.other_type[tcs[p]][ti];
+            tmp = cmul(tmp, s.a[((size_t)t2 * F + n) * La + M.term_lm[it][p]]);
+          }
+          feat += tmp.re;
+        }
+        d[f] = feat;
+      }
+      if (d_out) std::copy(d.begin(), d.end(), d_out + (size_t)i * D);
+      // polynomial features, mlipkk.cpp:1167-1179
+      if (p_out)
+        for (int pi = 0; pi < C; ++pi) {
+          double v = 1.0;
+          for (int f : M.poly[pi]) v *= d[f];
+          p_out[(size_t)i * C + pi] = v;
+        }
+      if (!ff_out && !sf_out) continue;
+      for (int q = off[i]; q < off[i + 1]; ++q) {
+        const int j = nbr[q];
+        const int tj = type[j];
+        if (tj < 0) continue;
+        const double dx = x[3 * j] - x[3 * i];
+        const double dy = x[3 * j + 1] - x[3 * i + 1];
+        const double dz = x[3 * j + 2] - x[3 * i + 2];
+        const double dis = std::sqrt(dx * dx + dy * dy + dz * dz);
+        if (dis > M.pot.cutoff) continue;
+        const double invdis = 1.0 / dis;
+        compute_sh(M, dz / dis, std::atan2(dy, dx), dis, true, w);
+        compute_fn(M, dis, fn, fnd);
+        const int tc_ij = M.type_pairs[ti][tj];
+        // dirj, mlipkk.cpp:1054-1150 (the centre's half of each pair)
+        std::fill(dirj.begin(), dirj.end(), 0.0);
+        for (int f = 0; f < D; ++f) {
+          const int itc = f % ITCn;
+          if (!M.itc[itc].inter[ti]) continue;
+          const int n = f / ITCn;
+          const auto& tcs = M.itc[itc].type_combs;
+          const int ir = M.itc[itc].irreps;
+          const int order = (int)tcs.size();
+          for (int term = 0; term < M.irr_nterms[ir]; ++term) {
+            const int it = M.irr_first[ir] + term;
+            for (int mu = 0; mu < order; ++mu) {
+              if (tcs[mu] != tc_ij) continue;
+              cplx tmp = {M.term_c[it], 0.0};
+              for (int mu2 = 0; mu2 < order; ++mu2) {
+                if (mu2 == mu) continue;
+                const int t2 = M.other_type[tcs[mu2]][ti];
+                tmp = cmul(tmp, s.a[((size_t)t2 * F + n) * La + M.term_lm[it][mu2]]);
+              }
+              const int lm_mu = M.term_lm[it][mu];
+              const int l_mu = M.lm_l[lm_mu], m_mu = M.lm_m[lm_mu];
+              cplx ylm, ydx, ydy, ydz;
+              if (m_mu > 0) {
+                const int lmi = l_mu * (l_mu + 1) / 2 + l_mu - m_mu;   // (l, -m)
+                const double sm = (m_mu % 2) ? -1.0 : 1.0;
+                ylm = {sm * w.ylm[lmi].re, -sm * w.ylm[lmi].im};
+                ydx = {sm * w.dx[lmi].re, -sm * w.dx[lmi].im};
+                ydy = {sm * w.dy[lmi].re, -sm * w.dy[lmi].im};
+                ydz = {sm * w.dz[lmi].re, -sm * w.dz[lmi].im};
+              } else {
+                const int lmi = l_mu * (l_mu + 1) / 2 + l_mu + m_mu;
+                ylm = w.ylm[lmi];
+                ydx = w.dx[lmi];
+                ydy = w.dy[lmi];
+                ydz = w.dz[lmi];
+              }
+              const cplx f1 = cscale(ylm, fnd[n]);
+              cplx bx = {f1.re * dx * invdis + fn[n] * ydx.re, f1.im * dx * invdis + fn[n] * ydx.im};
+              cplx by = {f1.re * dy * invdis + fn[n] * ydy.re, f1.im * dy * invdis + fn[n] * ydy.im};
+              cplx bz = {f1.re * dz * invdis + fn[n] * ydz.re, f1.im * dz * invdis + fn[n] * ydz.im};
+              bx.im *= -1;
+              by.im *= -1;
+              bz.im *= -1;
+              dirj[(size_t)f * 3] += prod_real(tmp, bx);
+              dirj[(size_t)f * 3 + 1] += prod_real(tmp, by);
+              dirj[(size_t)f * 3 + 2] += prod_real(tmp, bz);
+            }
+          }
+        }
+        // force and stress features, mlipkk.cpp:1217-1273
+        for (int pi = 0; pi < C; ++pi) {
+          const vi& row = M.poly[pi];
+          double t3[3] = {0, 0, 0};
+          for (size_t nu = 0; nu < row.size(); ++nu) {
+            double prod = 1.0;
+            for (size_t nu2 = 0; nu2 < row.size(); ++nu2)
+              if (nu2 != nu) prod *= d[row[nu2]];
+            for (int k = 0; k < 3; ++k) t3[k] += dirj[(size_t)row[nu] * 3 + k] * prod;
+          }
+          if (ff_out) {
+            for (int k = 0; k < 3; ++k) {
+              ffl[((size_t)i * C + pi) * 3 + k] += t3[k];
+              ffl[((size_t)j * C + pi) * 3 + k] -= t3[k];
+            }
+          }
+          if (sf_out) {
+            double* sp = &sfl[(size_t)pi * 6];
+            sp[0] -= dx * t3[0]; sp[1] -= dy * t3[1]; sp[2] -= dz * t3[2];
+            sp[3] -= dy * t3[2]; sp[4] -= dz * t3[0]; sp[5] -= dx * t3[1];
+          }
+        }
+      }
+    }
+  }
+  for (int t = 0; t < nth; ++t) {
+    if (ff_out && !ffb[t].empty())
+      for (size_t k = 0; k < ffb[t].size(); ++k) ff_out[k] += ffb[t][k];
+    if (sf_out && !sfb[t].empty())
+      for (size_t k = 0; k < sfb[t].size(); ++k) sf_out[k] += sfb[t][k];
+  }
   return 0;
 }
 

@@ -52,6 +52,9 @@ def lib():
         L.orc_compute.restype = ctypes.c_int
         L.orc_compute.argtypes = [P, ctypes.c_int, ctypes.c_int, dp, ip, ip, ip, dp, dp, dp,
                                   dp, dp]
+        L.orc_coeffs.argtypes = [P, dp]
+        L.orc_features.restype = ctypes.c_int
+        L.orc_features.argtypes = [P, ctypes.c_int, ctypes.c_int, dp, ip, ip, ip, dp, dp, dp, dp]
         L.orc_linear_conditioning.restype = ctypes.c_int
         L.orc_linear_conditioning.argtypes = [P, ctypes.c_int, ctypes.c_int, dp, ip, ip, ip, dp]
         L.orc_compute_centers.restype = ctypes.c_int
@@ -142,6 +145,40 @@ class Oracle:
             a = an[0::2] + 1j * an[1::2]
             out["anlm"] = a.reshape(sysm.nlocal, i["T"], i["F"], i["Lh"])
         return out
+
+    def features(self, sysm, want=("d", "p", "ff", "sf")):
+        """Training features (reference semantics): structural d [nlocal, D],
+        polynomial p [nlocal, C], force ff [nlocal, C, 3] (ghost rows folded onto
+        their owners) and stress sf [C, 6] (order xx yy zz yz zx xy)."""
+        x = np.ascontiguousarray(sysm.x, dtype=np.float64)
+        t = np.ascontiguousarray(sysm.type, dtype=np.int32)
+        off = np.ascontiguousarray(sysm.nbr_off, dtype=np.int32)
+        nb = np.ascontiguousarray(sysm.nbr_idx, dtype=np.int32)
+        D, C = self.info["D"], self.info["n_coeffs"]
+        d = np.zeros((sysm.nlocal, D)) if "d" in want else None
+        p = np.zeros((sysm.nlocal, C)) if "p" in want else None
+        ff = np.zeros((sysm.nall, C, 3)) if "ff" in want else None
+        sf = np.zeros((C, 6)) if "sf" in want else None
+        lib().orc_features(self.h, sysm.nlocal, sysm.nall, _dp(x), _ip(t), _ip(off), _ip(nb),
+                           *[(_dp(a) if a is not None else None) for a in (d, p, ff, sf)])
+        out = {}
+        if d is not None:
+            out["d"] = d
+        if p is not None:
+            out["p"] = p
+        if ff is not None:
+            folded = np.zeros((sysm.nlocal, C, 3))
+            np.add.at(folded, sysm.owner, ff)
+            out["ff"] = folded
+        if sf is not None:
+            out["sf"] = sf
+        return out
+
+    def coefficients(self):
+        """The potential's regression coefficients (divided by their scales)."""
+        w = np.zeros(self.info["n_coeffs"])
+        lib().orc_coeffs(self.h, _dp(w))
+        return w
 
     def linear_conditioning(self, sysm):
         """Per owned atom: sum over linear-only features of |w_f| sum_terms |c| prod |a|

@@ -146,3 +146,24 @@ def test_high_l_models(tmp_path, maxl, order, gl):
             c2.positions[a, k] += sgn * h
             e.append(o.compute(build_system(c2, o.cutoff, skin=1.0))["energy"])
         assert F[a, k] == pytest.approx(-(e[0] - e[1]) / (2 * h), abs=1e-6)
+
+
+@pytest.mark.parametrize("pot", ["gtinv-820", "gtinv-434"])
+def test_training_features_identities(potdir, pot):
+    """The oracle's training features (the reference's prepare_features:
+    structural, polynomial, force and stress features) reproduce its energy,
+    forces and virial through the linear model: E = sum_i P_i . w,
+    F = FF . w, virial = SF . w."""
+    o = Oracle(potdir[pot], threads=8)
+    s = build_system(structure("structure.lammps"), o.cutoff, skin=2.0)
+    ft = o.features(s)
+    ref = o.compute(s)
+    w = o.coefficients()
+    assert ft["p"].sum(0) @ w == pytest.approx(ref["energy"], rel=1e-12)
+    np.testing.assert_allclose(ft["p"] @ w, ref["eatom"], rtol=0, atol=1e-10)
+    F = np.einsum("ipk,p->ik", ft["ff"], w)
+    Fr = s.fold_forces(ref["f_all"])
+    assert np.abs(F - Fr).max() <= 1e-11 * np.abs(Fr).max()
+    v = w @ ft["sf"]                       # xx yy zz yz zx xy
+    vr = ref["virial"]                     # xx yy zz xy xz yz
+    assert np.abs(v[[0, 1, 2, 5, 4, 3]] - vr).max() <= 1e-10 * np.abs(vr).max()
