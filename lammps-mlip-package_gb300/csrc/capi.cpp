@@ -89,6 +89,7 @@ struct mlipg_handle {
   DevBuf d_terms_f;   // the same terms with the coefficient as FP32 (mixed path)
   DevBuf d_iunits, d_iunit_off, d_tuples, d_wlin_f, d_phase, d_adj_base, d_adj_off, d_adj;
   DevBuf d_radial_rec;   // FP64 radial recurrence constants (common beta), or empty
+  DevBuf d_pair_terms, d_pair_term_off, d_pair_adj, d_pair_adj_off, d_type_pairs;
   double rec_q = 0.0;
   // per-call buffers (grow only)
   DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_vatom, d_partials, d_status, d_out8;
@@ -222,6 +223,13 @@ static int upload_model(mlipg_handle* h) {
     CK(upload(h->d_wlin_f, wf, s), "upload linear weights (FP32)");
   }
   CK(upload(h->d_radial, radial, s), "upload radial parameters");
+  if (M.pot.pair) {
+    CK(upload(h->d_pair_terms, M.pair_terms, s), "upload pair terms");
+    CK(upload(h->d_pair_term_off, M.pair_term_off, s), "upload pair term offsets");
+    CK(upload(h->d_pair_adj, M.pair_adj, s), "upload pair adjoint records");
+    CK(upload(h->d_pair_adj_off, M.pair_adj_off, s), "upload pair adjoint offsets");
+    CK(upload(h->d_type_pairs, M.type_pairs, s), "upload type pairs");
+  }
   {
     // Common beta: f_{n+1} = f_n exp(-beta (mu_{n+1} - mu_n)(mu_{n+1} + mu_n - 2r)),
     // written with the mean spacing d as exp(2 beta d r) * K_n * exp(eps_n r),
@@ -321,6 +329,8 @@ int mlipg_destroy(mlipg_handle* h) {
                     &h->d_terms, &h->d_terms_f, &h->d_units, &h->d_unit_off, &h->d_nl,
                     &h->d_nl_off,
                     &h->d_poly, &h->d_poly_off, &h->d_wlin, &h->d_radial, &h->d_radial_rec,
+                    &h->d_pair_terms, &h->d_pair_term_off, &h->d_pair_adj, &h->d_pair_adj_off,
+                    &h->d_type_pairs,
                     &h->d_x4,
                     &h->d_centers, &h->d_off, &h->d_idx, &h->d_f, &h->d_eatom, &h->d_vatom, &h->d_partials,
                     &h->d_status, &h->d_out8};
@@ -422,6 +432,13 @@ static int effective_nb_cap(int nb_cap) {
 // handle's model, precision and neighbour capacity.
 static int kernel_shape(mlipg_handle* h, int nb_cap, size_t* smem, int* bps) {
   const Model& M = h->model;
+  if (M.pot.pair) {
+    // the radial-only kernel: FP64 in every precision, no neighbour capacity
+    *smem = pair_smem_bytes(M.F, M.D);
+    *bps = pair_max_blocks(*smem);
+    if (*bps < 1) return fail(h, MLIPG_ENOTSUP, "pair kernel cannot be resident (smem %zu)", *smem);
+    return MLIPG_OK;
+  }
   const bool fp64 = h->precision == MLIPG_PREC_FP64;
   *smem = fused_smem_bytes(fp64, M.T, M.L, nb_cap, std::max(M.max_nl, 1), fp64 ? 0 : M.lh64);
   if (*smem > 227 * 1024)
@@ -496,6 +513,12 @@ static int launch_eval(mlipg_handle* h, int ncenters, const double4* x4, const i
   a.w_lin_f = h->d_wlin_f.as<float>();
   a.phase_clocks = h->profiling ? h->d_phase.as<unsigned long long>() : nullptr;
   a.radial = h->d_radial.as<double>();
+  a.pair_terms = h->d_pair_terms.as<DevicePairTerm>();
+  a.pair_term_off = h->d_pair_term_off.as<int>();
+  a.pair_adj = h->d_pair_adj.as<DevicePairAdj>();
+  a.pair_adj_off = h->d_pair_adj_off.as<int>();
+  a.type_pairs = h->d_type_pairs.as<int>();
+  a.pair_nd = M.pot.pair ? M.D : 0;
   a.radial_rec = h->d_radial_rec.as<double>();
   a.rec_q = h->rec_q;
   a.T = M.T;
@@ -526,7 +549,9 @@ static int launch_eval(mlipg_handle* h, int ncenters, const double4* x4, const i
     }
     CK(cudaEventRecord(ev0, h->stream), "event record");
   }
-  if (ncenters > 0) {
+  if (ncenters > 0 && M.pot.pair) {
+    CK(launch_pair(a, grid, smem, h->stream), "pair kernel launch");
+  } else if (ncenters > 0) {
     CK(launch_fused(fp64, M.L, a, grid, smem, h->stream), "fused kernel launch");
   } else {
     CK(cudaMemsetAsync(partials, 0, 8 * sizeof(double), h->stream), "memset partials");
@@ -843,6 +868,10 @@ extern "C" int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4,
   if (ncenters <= 0 || !d_x4 || !d_centers || !d_nbr_off || !d_nbr_idx || !d_f || !d_out8)
     return fail(h, MLIPG_EINVAL, "mlipg_autotune: invalid arguments");
   const Model& M = h->model;
+  if (M.pot.pair) {   // the radial-only kernel has no tile shape to choose
+    if (nreport) *nreport = 0;
+    return MLIPG_OK;
+  }
   const bool fp64 = h->precision == MLIPG_PREC_FP64;
   const int cap = effective_nb_cap(nb_cap);
   const size_t smem =

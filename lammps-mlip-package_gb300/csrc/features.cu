@@ -519,6 +519,10 @@ extern "C" int mlipg_features(mlipg_handle* h, int natoms, const double* lattice
   cudaStream_t s = static_cast<cudaStream_t>(mlipg_stream(h));
   if (!s) return mlipg_internal_fail(h, MLIPG_ENOGPU, "no CUDA device is available");
   const Model& M = *mlipg_internal_model(h);
+  if (M.pot.pair)
+    return mlipg_internal_fail(h, MLIPG_ENOTSUP,
+                               "mlipg_features: training features are defined for invariant "
+                               "(gtinv) potentials");
   for (int i = 0; i < natoms; ++i)
     if (elements[i] < 0 || elements[i] >= M.T)
       return mlipg_internal_fail(h, MLIPG_EINVAL, "mlipg_features: element index out of range");

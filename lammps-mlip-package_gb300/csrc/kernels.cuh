@@ -48,6 +48,13 @@ struct KernelArgs {
   const double* w_lin;    // [n_itc][16]
   const float* w_lin_f;   // [n_itc][16], FP32 copy for the mixed path
   const double* radial;   // [F][2] (beta, mu)
+  // radial-only descriptor (pair potentials, pair.cu)
+  const DevicePairTerm* pair_terms;
+  const int* pair_term_off;      // [T + 1]
+  const DevicePairAdj* pair_adj;
+  const int* pair_adj_off;       // [T * pair_nd + 1]
+  const int* type_pairs;         // [T][T] -> type pair index
+  int pair_nd;                   // features: type pairs x radial functions
   // Optional recurrence of the FP64 radial functions for a common beta
   // (null: one exp per function): f_{n+1}/fc = f_n/fc * exp(rec_q r) *
   // K_n * (1 + eps_n r), radial_rec[n] = (K_n, eps_n)
@@ -77,6 +84,11 @@ cudaError_t launch_fused(bool fp64, int L, const KernelArgs& a, int grid, size_t
 cudaError_t launch_finalize(const double* partials, int nparts, const int* status, double* out8,
                             cudaStream_t s);
 cudaError_t init_device_constants();
+
+// radial-only descriptor kernel (pair.cu)
+size_t pair_smem_bytes(int F, int nd);
+int pair_max_blocks(size_t smem);
+cudaError_t launch_pair(const KernelArgs& a, int grid, size_t smem, cudaStream_t s);
 
 }  // namespace mlipg
 

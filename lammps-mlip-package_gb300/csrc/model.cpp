@@ -565,6 +565,7 @@ bool schedules_for_tiling(Model& M, std::string& err) {
 }  // namespace
 
 bool build_schedules(Model& M, std::string& err) {
+  if (M.pot.pair) return true;   // the radial-only kernel has no tile shape
   if (M.tiling.irr_chunk < 2 || M.tiling.irr_chunk > 4096 || M.tiling.irr_chunk % 2 ||
       M.tiling.warp_order < 0 || M.tiling.warp_order > 2 || M.tiling.ctas_per_sm < 0) {
     err = "invalid tiling";
@@ -611,33 +612,36 @@ bool read_potential(const std::string& path, Potential& p, std::string& err) {
   }
   if (!getline_ss(in, ss, err)) return false;
   ss >> s;
-  if (s == "pair") {
-    err = "NotImplemented: des_type == pair";
-    return false;
-  }
-  if (s != "gtinv") {
+  if (s != "gtinv" && s != "pair") {
     err = "Unknown des_type: " + s;
     return false;
   }
+  p.pair = s == "pair";
   if (!getline_ss(in, ss, err)) return false;
   ss >> p.model_type;
   if (!getline_ss(in, ss, err)) return false;
   ss >> p.maxp;
   if (!getline_ss(in, ss, err)) return false;
   ss >> p.maxl;
-  if (!getline_ss(in, ss, err)) return false;
-  ss >> p.gtinv_order;
-  const int nm = p.gtinv_order - 1;
-  if (nm < 0 || nm > kMaxOrder - 1) {
-    err = "gtinv_order out of range";
-    return false;
+  if (p.pair) {
+    // the radial-only descriptor's file has no invariant lines
+    // (src/USER-MLIP/mlip_model.h:61-74)
+    p.gtinv_order = 1;
+  } else {
+    if (!getline_ss(in, ss, err)) return false;
+    ss >> p.gtinv_order;
+    const int nm = p.gtinv_order - 1;
+    if (nm < 0 || nm > kMaxOrder - 1) {
+      err = "gtinv_order out of range";
+      return false;
+    }
+    if (!getline_ss(in, ss, err)) return false;
+    p.gtinv_maxl.assign(nm, 0);
+    for (auto& v : p.gtinv_maxl) ss >> v;
+    if (!getline_ss(in, ss, err)) return false;
+    p.gtinv_sym.assign(nm, 0);
+    for (auto& v : p.gtinv_sym) ss >> v;
   }
-  if (!getline_ss(in, ss, err)) return false;
-  p.gtinv_maxl.assign(nm, 0);
-  for (auto& v : p.gtinv_maxl) ss >> v;
-  if (!getline_ss(in, ss, err)) return false;
-  p.gtinv_sym.assign(nm, 0);
-  for (auto& v : p.gtinv_sym) ss >> v;
   long nc = 0;
   if (!getline_ss(in, ss, err)) return false;
   ss >> nc;
@@ -673,9 +677,132 @@ bool read_potential(const std::string& path, Potential& p, std::string& err) {
   return true;
 }
 
+// Radial-only descriptor of the legacy `pair_style mlip_pair`: feature
+// index tc * F + n, with the type pairs tc ordered (a, b), a <= b
+// (src/USER-MLIP/mlip_model_params.cpp:29-34); coefficient order: the linear
+// terms, then the second- and third-order terms -- every feature squared and
+// cubed for model_type 1 (mlip_polynomial.cpp:33-38), for model_type 2 the
+// multisets of features whose type pairs share an element, enumerated
+// i1 >= i2 (>= i3) (mlip_model_params.cpp:180-213); model_types 3 and 4 are
+// linear for this descriptor (mlip_model_params.cpp:42-66).  The legacy
+// reader doubles the coefficients (mlip_model.h:90) and its half-list pair
+// sums count each term twice, so the per-atom energy is the plain polynomial
+// of dn with coefficient / scale.
+bool build_pair_model(Model& M, std::string& err) {
+  const Potential& p = M.pot;
+  const int T = M.T, F = M.F;
+  if (T < 1 || T > 2) {
+    err = "the pair descriptor supports one or two elements";
+    return false;
+  }
+  if (F < 1 || F > kPairMaxF) {
+    err = "number of radial functions of a pair potential must be in [1, 64]";
+    return false;
+  }
+  M.TC = T * (T + 1) / 2;
+  std::vector<std::pair<int, int>> tcs;
+  for (int a = 0; a < T; ++a)
+    for (int b = a; b < T; ++b) tcs.push_back({a, b});
+  M.type_pairs.assign(T * T, 0);
+  for (int tc = 0; tc < M.TC; ++tc) {
+    M.type_pairs[tcs[tc].first * T + tcs[tc].second] = tc;
+    M.type_pairs[tcs[tc].second * T + tcs[tc].first] = tc;
+  }
+  const int nd = F * M.TC;
+  const auto has = [&](int seq, int t) {
+    return tcs[seq / F].first == t || tcs[seq / F].second == t;
+  };
+  const auto shared = [&](const std::vector<int>& seqs) {
+    for (int t = 0; t < T; ++t) {
+      bool all = true;
+      for (int q : seqs) all = all && has(q, t);
+      if (all) return true;
+    }
+    return false;
+  };
+  M.poly.clear();
+  for (int n = 0; n < nd; ++n) M.poly.push_back({n});
+  if (p.model_type == 1) {
+    if (p.maxp > 1) for (int n = 0; n < nd; ++n) M.poly.push_back({n, n});
+    if (p.maxp > 2) for (int n = 0; n < nd; ++n) M.poly.push_back({n, n, n});
+  } else if (p.model_type == 2) {
+    if (p.maxp > 1)
+      for (int i1 = 0; i1 < nd; ++i1)
+        for (int i2 = 0; i2 <= i1; ++i2)
+          if (shared({i1, i2})) M.poly.push_back({i2, i1});
+    if (p.maxp > 2)
+      for (int i1 = 0; i1 < nd; ++i1)
+        for (int i2 = 0; i2 <= i1; ++i2)
+          for (int i3 = 0; i3 <= i2; ++i3)
+            if (shared({i1, i2, i3})) M.poly.push_back({i3, i2, i1});
+  } else if (p.model_type < 1 || p.model_type > 4) {
+    err = "Unknown model_type: " + std::to_string(p.model_type);
+    return false;
+  }
+  if (M.poly.size() != p.coeffs.size()) {
+    char b[200];
+    snprintf(b, sizeof b, "number of regression coefficients %zu does not match the model (%zu)",
+             p.coeffs.size(), M.poly.size());
+    err = b;
+    return false;
+  }
+  M.D = nd;
+  // per centre element: the terms whose type pairs all contain it (the
+  // others multiply a feature that is zero for it), and the adjoint records
+  M.pair_terms.clear();
+  M.pair_term_off.assign(T + 1, 0);
+  M.pair_adj.clear();
+  M.pair_adj_off.assign((size_t)T * nd + 1, 0);
+  for (int t = 0; t < T; ++t) {
+    M.pair_term_off[t] = (int)M.pair_terms.size();
+    std::vector<std::vector<DevicePairAdj>> adj(nd);
+    for (size_t k = 0; k < M.poly.size(); ++k) {
+      const auto& row = M.poly[k];
+      bool ok = true;
+      for (int q : row) ok = ok && has(q, t);
+      if (!ok) continue;
+      DevicePairTerm dt{};
+      dt.c = p.coeffs[k];
+      dt.order = (int)row.size();
+      for (int q = 0; q < 3; ++q) dt.f[q] = q < dt.order ? row[q] : -1;
+      M.pair_terms.push_back(dt);
+      for (int a = 0; a < dt.order; ++a) {
+        DevicePairAdj r{};
+        r.c = dt.c;
+        int o = 0;
+        for (int b = 0; b < dt.order; ++b)
+          if (b != a) r.other[o++] = row[b];
+        for (; o < 2; ++o) r.other[o] = -1;
+        adj[row[a]].push_back(r);
+      }
+    }
+    for (int f = 0; f < nd; ++f) {
+      M.pair_adj.insert(M.pair_adj.end(), adj[f].begin(), adj[f].end());
+      M.pair_adj_off[(size_t)t * nd + f + 1] = (int)M.pair_adj.size();
+    }
+  }
+  M.pair_term_off[T] = (int)M.pair_terms.size();
+  if (nd > kBlockThreads) {
+    err = "too many pair features for the kernel";
+    return false;
+  }
+  return true;
+}
+
 bool build_model(Model& M, std::string& err) {
   const Potential& p = M.pot;
   M.T = (int)p.elements.size();
+  if (p.pair) {
+    M.F = (int)p.params.size();
+    M.L = 0;
+    M.Lh = 1;
+    if (p.cutoff <= 0) {
+      err = "cutoff must be positive";
+      return false;
+    }
+    M.sched.assign(M.T, Schedule());   // no tile schedules: one empty per element
+    return build_pair_model(M, err);
+  }
   if (M.T > kMaxTypes) {
     err = "more than 8 elements are not supported";
     return false;
@@ -808,6 +935,17 @@ bool count_coefficients(int n_types, int model_type, int maxp, int maxl, int gti
 }
 
 double flops_per_atom_step(const Model& M, int t, double nbar) {
+  if (M.pot.pair) {
+    // radial-only descriptor: per neighbour and radial function the feature
+    // sum (1) and the force contraction (2 + 3); the polynomial and its
+    // adjoint per valid term
+    double f = nbar * M.F * 6.0;
+    for (int k = M.pair_term_off[t]; k < M.pair_term_off[t + 1]; ++k) {
+      const double p = M.pair_terms[k].order;
+      f += 2.0 * p + 2.0 * p * (p - 1.0);
+    }
+    return f;
+  }
   double f = nbar * M.F * M.Lh * (4.0 + 30.0);
   for (int i = 0; i < M.n_itc; ++i) {
     if (!M.itc[i].inter[t]) continue;

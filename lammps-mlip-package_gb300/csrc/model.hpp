@@ -24,6 +24,7 @@ constexpr int kMaxL = 20;      // coupling table angular momenta <= 20
 constexpr int kMaxTypes = 8;
 
 struct Potential {
+  bool pair = false;       // des_type "pair": the radial-only descriptor
   std::vector<std::string> elements;
   std::vector<double> masses;
   double cutoff = 0;
@@ -111,6 +112,22 @@ struct Tiling {
   int ctas_per_sm = 0;
 };
 
+// Radial-only descriptor ("pair" potentials): features
+// dn[tc * F + n] = sum_j f_n(r_ij) over neighbours j with type pair
+// tc = tc(t_i, t_j), energy E_i = sum_k c_k prod_{f in term k} dn[f].
+constexpr int kPairMaxF = 64;     // radial functions of a pair potential
+constexpr int kBlockThreads = 256;  // threads of the pair kernel's CTA (one per feature)
+struct DevicePairTerm {   // 32 bytes: one polynomial term valid for a centre element
+  double c;
+  int f[3];               // feature indices, -1 past the order
+  int order;
+  int pad[2];
+};
+struct DevicePairAdj {    // 16 bytes: dE/d dn[f] += c * prod dn[other]
+  double c;
+  int other[2];           // -1 past the term's order - 1
+};
+
 struct ITC {
   int irreps;
   std::vector<int> type_combs;
@@ -152,6 +169,13 @@ struct Model {
   // order parameters the mixed path evaluates in FP64 for the polynomial's
   // input features; 0 when the model has no polynomial terms of order >= 2
   int lh64 = 0;
+  // radial-only descriptor: per centre element, its valid terms and, per
+  // feature, the (weight, other factors) records of dE/d dn (CSR over
+  // element * n_features + feature)
+  std::vector<DevicePairTerm> pair_terms;
+  std::vector<int> pair_term_off;        // [T + 1]
+  std::vector<DevicePairAdj> pair_adj;
+  std::vector<int> pair_adj_off;         // [T * TC * F + 1]
   // Largest scaled adjoint flush allowed in the mixed path's fixed-point
   // adjoint accumulation (high parts in multiples of 2^16): a power of two with
   // (flushes per entry) x bound / 2^16 < 2^31, so no integer sum overflows.

@@ -7,11 +7,15 @@
      pair_style mlip_gtinv/gpu            (no arguments)
      pair_coeff * * mlp.lammps El1 ... ElN   (one element or NULL per type)
    With `-sf gpu`, `pair_style mlip_gtinv` resolves to this style.
+   The same class serves `mlip_pair/gpu`, the drop-in for the reference's
+   radial-only `pair_style mlip_pair` (pair_mlip_pair.h): the potential
+   file's des_type line selects the descriptor.
    Requires atom IDs, `newton_pair on` and requests a full neighbour list.
 ------------------------------------------------------------------------- */
 #ifdef PAIR_CLASS
 // clang-format off
 PairStyle(mlip_gtinv/gpu, PairMLIPGtinvGPU);
+PairStyle(mlip_pair/gpu, PairMLIPGtinvGPU);
 // clang-format on
 #else
 

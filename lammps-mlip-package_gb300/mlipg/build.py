@@ -55,6 +55,7 @@ def _sources():
         "batch.o": ("nvcc", os.path.join(CSRC, "batch.cu")),
         "dnlist.o": ("nvcc", os.path.join(CSRC, "dnlist.cu")),
         "features.o": ("nvcc", os.path.join(CSRC, "features.cu")),
+        "pair.o": ("nvcc", os.path.join(CSRC, "pair.cu")),
         "kernels_f64.o": ("nvcc", os.path.join(CSRC, "kernels_f64.cu")),
         "kernels_f32.o": ("nvcc", os.path.join(CSRC, "kernels_f32.cu")),
     }

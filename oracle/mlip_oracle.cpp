@@ -25,6 +25,14 @@
 // with the same loop order and complex-product association, so results agree
 // with the reference to rounding of the summation order.
 //
+// Potentials of the radial-only descriptor (des_type "pair", the reference's
+// `pair_style mlip_pair`) follow the legacy pair style instead:
+//   file reader          src/USER-MLIP/mlip_model.h:31-112 (coefficients x2/scale)
+//   enumeration          src/USER-MLIP/mlip_model_params.cpp:26-81, 180-213
+//   power terms          src/USER-MLIP/mlip_polynomial.cpp:33-43
+//   energy and forces    src/USER-MLIP/pair_mlip_pair.cpp:56-264
+// restated in the owner-computes form (orc_pair_compute).
+//
 // A second entry point, orc_compute_centers, evaluates the same physics for
 // a subset of centre atoms in the owner-computes form (each centre scatters
 // only its own adjoint onto its neighbours).  It is used to time the CPU
@@ -67,6 +75,7 @@ std::string g_err;
 
 // ---------------------------------------------------------------- parser
 struct Potential {
+  bool pair = false;              // des_type "pair" (radial-only descriptor)
   std::vector<std::string> elements;
   double cutoff = 0;
   int model_type = 0, maxp = 0, maxl = 0, gtinv_order = 0;
@@ -113,22 +122,28 @@ bool read_potential(const char* path, Potential& p) {
   if (s != "gaussian") { g_err = "Unknown pair_type: " + s; return false; }
   if (!get_line(ss)) return false;
   ss >> s;
-  if (s != "gtinv") { g_err = "Unsupported des_type: " + s; return false; }
+  if (s != "gtinv" && s != "pair") { g_err = "Unsupported des_type: " + s; return false; }
+  p.pair = s == "pair";
   if (!get_line(ss)) return false;
   ss >> p.model_type;
   if (!get_line(ss)) return false;
   ss >> p.maxp;
   if (!get_line(ss)) return false;
   ss >> p.maxl;
-  if (!get_line(ss)) return false;
-  ss >> p.gtinv_order;
-  const int nm = p.gtinv_order - 1;
-  if (!get_line(ss)) return false;
-  p.gtinv_maxl.assign(nm, 0);
-  for (int k = 0; k < nm; ++k) ss >> p.gtinv_maxl[k];
-  if (!get_line(ss)) return false;
-  p.gtinv_sym.assign(nm, 0);
-  for (int k = 0; k < nm; ++k) ss >> p.gtinv_sym[k];
+  if (p.pair) {
+    // the pair descriptor's file has no invariant lines (mlip_model.h:61-74)
+    p.gtinv_order = 1;
+  } else {
+    if (!get_line(ss)) return false;
+    ss >> p.gtinv_order;
+    const int nm = p.gtinv_order - 1;
+    if (!get_line(ss)) return false;
+    p.gtinv_maxl.assign(nm, 0);
+    for (int k = 0; k < nm; ++k) ss >> p.gtinv_maxl[k];
+    if (!get_line(ss)) return false;
+    p.gtinv_sym.assign(nm, 0);
+    for (int k = 0; k < nm; ++k) ss >> p.gtinv_sym[k];
+  }
   int nc = 0;
   if (!get_line(ss)) return false;
   ss >> nc;
@@ -704,8 +719,71 @@ struct PairForce {
   double fx, fy, fz;
 };
 
+// ------------------------------------------------ radial-only descriptor
+// Legacy pair model: features dn[tc * F + n] = sum_j f_n(r_ij) over the
+// neighbours j with type pair tc = tc(t_i, t_j), and a polynomial in them.
+struct PairModel {
+  int T = 0, F = 0, TC = 0;
+  vvi tc_types;            // [tc] -> {a, b}, a <= b (type_comb_pair order)
+  vvi pair_tc;             // [t1][t2] -> tc
+  vvi terms;               // coefficient index -> feature seqs (tc * F + n)
+};
+
+// mlip_model_params.cpp:29-71 (type_comb_pair: one entry per a <= b),
+// 180-213 (combination2 / combination3), mlip_polynomial.cpp:33-43 (powers)
+bool build_pair_model(const Potential& p, PairModel& P) {
+  P.T = (int)p.elements.size();
+  P.F = (int)p.params.size();
+  if (P.T < 1 || P.T > 2) {
+    g_err = "the pair descriptor supports one or two elements";
+    return false;
+  }
+  for (int a = 0; a < P.T; ++a)
+    for (int b = a; b < P.T; ++b) P.tc_types.push_back({a, b});
+  P.TC = (int)P.tc_types.size();
+  P.pair_tc.assign(P.T, vi(P.T, 0));
+  for (int tc = 0; tc < P.TC; ++tc) {
+    P.pair_tc[P.tc_types[tc][0]][P.tc_types[tc][1]] = tc;
+    P.pair_tc[P.tc_types[tc][1]][P.tc_types[tc][0]] = tc;
+  }
+  const int nd = P.F * P.TC;
+  const auto has = [&](int tc, int t) { return P.tc_types[tc][0] == t || P.tc_types[tc][1] == t; };
+  const auto shared = [&](std::initializer_list<int> seqs) {
+    for (int t = 0; t < P.T; ++t) {
+      bool all = true;
+      for (int q : seqs) all = all && has(q / P.F, t);
+      if (all) return true;
+    }
+    return false;
+  };
+  for (int n = 0; n < nd; ++n) P.terms.push_back({n});
+  if (p.model_type == 1) {
+    if (p.maxp > 1) for (int n = 0; n < nd; ++n) P.terms.push_back({n, n});
+    if (p.maxp > 2) for (int n = 0; n < nd; ++n) P.terms.push_back({n, n, n});
+  } else if (p.model_type == 2) {
+    if (p.maxp > 1)
+      for (int i1 = 0; i1 < nd; ++i1)
+        for (int i2 = 0; i2 <= i1; ++i2)
+          if (shared({i1, i2})) P.terms.push_back({i2, i1});
+    if (p.maxp > 2)
+      for (int i1 = 0; i1 < nd; ++i1)
+        for (int i2 = 0; i2 <= i1; ++i2)
+          for (int i3 = 0; i3 <= i2; ++i3)
+            if (shared({i1, i2, i3})) P.terms.push_back({i3, i2, i1});
+  }
+  if (P.terms.size() != p.coeffs.size()) {
+    char b[200];
+    snprintf(b, sizeof b, "coefficient count mismatch: file %zu, pair model %zu",
+             p.coeffs.size(), P.terms.size());
+    g_err = b;
+    return false;
+  }
+  return true;
+}
+
 struct Oracle {
   Model M;
+  PairModel P;
   int nthreads = 1;
 };
 
@@ -717,6 +795,21 @@ const char* orc_last_error() { return g_err.c_str(); }
 
 void* orc_create(const char* pot_path, const char* table_path) {
   Oracle* o = new Oracle();
+  Potential probe;
+  if (!read_potential(pot_path, probe)) {
+    delete o;
+    return nullptr;
+  }
+  if (probe.pair) {
+    o->M.pot = probe;
+    o->M.T = (int)probe.elements.size();
+    o->M.F = (int)probe.params.size();
+    if (!build_pair_model(probe, o->P)) {
+      delete o;
+      return nullptr;
+    }
+    return o;
+  }
   if (!build_model(o->M, pot_path, table_path)) {
     delete o;
     return nullptr;
@@ -724,13 +817,107 @@ void* orc_create(const char* pot_path, const char* table_path) {
   return o;
 }
 
+int orc_is_pair(void* h) { return static_cast<Oracle*>(h)->M.pot.pair ? 1 : 0; }
+
+// The radial-only descriptor (pair_mlip_pair.cpp:56-264) on a full list with
+// ghost atoms, owner-computes: per owned atom i the features dn_i, its energy
+// E_i = sum_f c_f dn_i,f + sum_p c_p prod dn_i (c = file coefficient / scale:
+// the legacy reader doubles the coefficients, mlip_model.h:90, and its
+// half-list pair sums count every term twice over), and for every neighbour
+// j the force of E_i, f = dE_i/dr_ij = sum_n f_n'(r) dE_i/d dn_i[tc,n] r_hat,
+// scattered as F_i += f, F_j -= f, virial -= r_ij (x) f.
+int orc_pair_compute(void* h, int nlocal, int nall, const double* x, const int* type,
+                     const int* off, const int* nbr, double* f, double* energy, double* virial,
+                     double* eatom) {
+  Oracle* o = static_cast<Oracle*>(h);
+  const Potential& p = o->M.pot;
+  const PairModel& P = o->P;
+  const int F = P.F, nd = F * P.TC;
+  std::fill(f, f + (size_t)3 * nall, 0.0);
+  double E = 0.0, vir[6] = {0, 0, 0, 0, 0, 0};
+  std::vector<double> dn(nd), H(nd), fn, fnd;
+  Model Mr;
+  Mr.pot = p;
+  Mr.F = F;
+  for (int i = 0; i < nlocal; ++i) {
+    const int ti = type[i];
+    if (ti < 0) {
+      if (eatom) eatom[i] = 0.0;
+      continue;
+    }
+    std::fill(dn.begin(), dn.end(), 0.0);
+    for (int q = off[i]; q < off[i + 1]; ++q) {
+      const int j = nbr[q];
+      if (type[j] < 0) continue;
+      const double dx = x[3 * j] - x[3 * i], dy = x[3 * j + 1] - x[3 * i + 1],
+                   dz = x[3 * j + 2] - x[3 * i + 2];
+      const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+      if (r >= p.cutoff) continue;
+      compute_fn(Mr, r, fn, fnd);
+      const int tc = P.pair_tc[ti][type[j]];
+      for (int n = 0; n < F; ++n) dn[tc * F + n] += fn[n];
+    }
+    // energy and dE/d dn
+    double Ei = 0.0;
+    std::fill(H.begin(), H.end(), 0.0);
+    for (size_t k = 0; k < P.terms.size(); ++k) {
+      // (features of type pairs without t_i are zero, and so is every term
+      // that contains one)
+      const vi& row = P.terms[k];
+      double prod = p.coeffs[k];
+      for (int q : row) prod *= dn[q];
+      Ei += prod;
+      for (size_t a = 0; a < row.size(); ++a) {
+        double g = p.coeffs[k];
+        for (size_t b = 0; b < row.size(); ++b)
+          if (b != a) g *= dn[row[b]];
+        H[row[a]] += g;
+      }
+    }
+    E += Ei;
+    if (eatom) eatom[i] = Ei;
+    for (int q = off[i]; q < off[i + 1]; ++q) {
+      const int j = nbr[q];
+      if (type[j] < 0) continue;
+      const double dx = x[3 * j] - x[3 * i], dy = x[3 * j + 1] - x[3 * i + 1],
+                   dz = x[3 * j + 2] - x[3 * i + 2];
+      const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+      if (r >= p.cutoff) continue;
+      compute_fn(Mr, r, fn, fnd);
+      const int tc = P.pair_tc[ti][type[j]];
+      double g = 0.0;
+      for (int n = 0; n < F; ++n) g += fnd[n] * H[tc * F + n];
+      const double fx = g * dx / r, fy = g * dy / r, fz = g * dz / r;
+      f[3 * i] += fx; f[3 * i + 1] += fy; f[3 * i + 2] += fz;
+      f[3 * j] -= fx; f[3 * j + 1] -= fy; f[3 * j + 2] -= fz;
+      vir[0] -= dx * fx; vir[1] -= dy * fy; vir[2] -= dz * fz;
+      vir[3] -= dx * fy; vir[4] -= dx * fz; vir[5] -= dy * fz;
+    }
+  }
+  *energy = E;
+  for (int k = 0; k < 6; ++k) virial[k] = vir[k];   // LAMMPS order xx yy zz xy xz yz
+  return 0;
+}
+
 void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
 
 void orc_set_threads(void* h, int n) { static_cast<Oracle*>(h)->nthreads = n > 0 ? n : 1; }
 
 // Model sizes: [T, TC, F, L, Lh, La, n_irreps, n_terms, ITC, D, n_coeffs, model_type, maxp]
+int orc_pair_compute(void* h, int nlocal, int nall, const double* x, const int* type,
+                     const int* off, const int* nbr, double* f, double* energy, double* virial,
+                     double* eatom);
+
 void orc_info(void* h, int* out13, double* cutoff) {
   const Model& M = static_cast<Oracle*>(h)->M;
+  if (M.pot.pair) {
+    const PairModel& P = static_cast<Oracle*>(h)->P;
+    int v[13] = {P.T, P.TC, P.F, 0, 1, 1, 0, 0, P.TC, P.F * P.TC, (int)P.terms.size(),
+                 M.pot.model_type, M.pot.maxp};
+    std::memcpy(out13, v, sizeof v);
+    *cutoff = M.pot.cutoff;
+    return;
+  }
   int v[13] = {M.T, M.TC, M.F, M.L, M.Lh, M.La, (int)M.irr_l.size(), (int)M.term_c.size(),
                M.ITC_n, M.D, (int)M.poly.size(), M.pot.model_type, M.pot.maxp};
   std::memcpy(out13, v, sizeof v);
@@ -805,6 +992,8 @@ int orc_compute(void* h, int nlocal, int nall, const double* x, const int* type,
                 const int* off, const int* nbr, double* f, double* energy, double* virial,
                 double* eatom, double* anlm_out) {
   Oracle* o = static_cast<Oracle*>(h);
+  if (o->M.pot.pair)
+    return orc_pair_compute(h, nlocal, nall, x, type, off, nbr, f, energy, virial, eatom);
   const Model& M = o->M;
   const Geometry g{nlocal, nall, x, type, off, nbr};
   const int F = M.F, Lh = M.Lh, La = M.La, T = M.T;

@@ -30,7 +30,7 @@ def potdir(tmp_path_factory):
     """Decompressed regression potentials: {name: path}."""
     d = tmp_path_factory.mktemp("pots")
     out = {}
-    for name in ["gtinv-197", "gtinv-820", "gtinv-434"]:
+    for name in ["gtinv-197", "gtinv-820", "gtinv-434", "pair-60", "pair-17"]:
         p = d / (name + ".mlip")
         with gzip.open(os.path.join(GOLDEN, name + ".mlip.gz"), "rb") as fi, open(p, "wb") as fo:
             shutil.copyfileobj(fi, fo)

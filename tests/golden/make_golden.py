@@ -6,8 +6,9 @@ on the GPU host; the outputs of this script are committed):
     python tests/golden/make_golden.py [/path/to/reference]
 
 What it writes:
-* ``gtinv-{197,820,434}.mlip.gz`` -- the reference's regression potentials
-  (test/regression/*.mlip), gzip-compressed, unchanged.
+* ``gtinv-{197,820,434}.mlip.gz``, ``pair-{60,17}.mlip.gz`` -- the
+  reference's regression potentials (test/regression/*.mlip), gzip-compressed,
+  unchanged (the pair potentials drive its `pair_style mlip_pair` runs).
 * ``structure*.lammps`` -- the reference's 32-atom TiAl3 cell and the 64-atom
   conventional / triclinic cells (test/regression/).
 * ``golden.json`` --
@@ -40,9 +41,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 POTS = ["gtinv-197", "gtinv-820", "gtinv-434"]
+PAIR_POTS = ["pair-60", "pair-17"]
 STRUCTS = ["structure.lammps", "structure_00064_conventional.lammps",
            "structure_00064_triclinic.lammps"]
-DUMPS = ["dump.atom.gtinv-197", "dump.atom.gtinv-820", "dump.atom.gtinv-434"]
+DUMPS = ["dump.atom.gtinv-197", "dump.atom.gtinv-820", "dump.atom.gtinv-434",
+         "dump.atom.pair-60", "dump.atom.pair-17"]
 SH_DIRS = [(0.3, -0.4, 1.2), (-1.1, 0.2, -0.5), (0.7, 0.7, 0.0), (0.0, 0.0, 2.0),
            (1e-3, -2e-3, -1.5), (-0.25, -0.9, 0.35)]
 
@@ -133,7 +136,7 @@ def main():
     sys.path.insert(0, os.path.join(REPO, "lammps-mlip-package_gb300"))
     from mlipg.structures import read_lammps_data
 
-    for p in POTS:
+    for p in POTS + PAIR_POTS:
         with open(os.path.join(reg, p + ".mlip"), "rb") as fi, \
                 gzip.open(os.path.join(HERE, p + ".mlip.gz"), "wb", 9) as fo:
             shutil.copyfileobj(fi, fo)
@@ -146,7 +149,9 @@ def main():
                       ("gtinv-820", "log.lammps.gtinv-820"),
                       ("gtinv-434", "log.lammps.gtinv-434"),
                       ("gtinv-197-stress", "log.lammps.gtinv-197.stress.ev_tally"),
-                      ("gtinv-197-conv64", "log.lammps.gtinv-197.conv64")]:
+                      ("gtinv-197-conv64", "log.lammps.gtinv-197.conv64"),
+                      ("pair-60", "log.lammps.pair-60"),
+                      ("pair-17", "log.lammps.pair-17")]:
         vals, line = thermo_step0(os.path.join(reg, log))
         vals["cite"] = "test/regression/%s:%d" % (log, line)
         logs[name] = vals
@@ -157,7 +162,9 @@ def main():
     for name, log, dt in [("gtinv-197", "log.lammps.gtinv-197", 0.001),
                           ("gtinv-820", "log.lammps.gtinv-820", 0.001),
                           ("gtinv-434", "log.lammps.gtinv-434", 0.001),
-                          ("gtinv-197-stress", "log.lammps.gtinv-197.stress.ev_tally", 0.005)]:
+                          ("gtinv-197-stress", "log.lammps.gtinv-197.stress.ev_tally", 0.005),
+                          ("pair-60", "log.lammps.pair-60", 0.001),
+                          ("pair-17", "log.lammps.pair-17", 0.001)]:
         rows = thermo_rows(os.path.join(reg, log))
         traj[name] = {"dt": dt, "rows": {str(k): v for k, v in rows.items()}}
     gold["nve"] = traj

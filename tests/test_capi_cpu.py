@@ -94,9 +94,24 @@ def test_bad_potential_files(tmp_path):
         mlipg.Potential(str(tmp_path / "missing.mlip"))
     assert e.value.code == 2
     bad = tmp_path / "bad.mlip"
-    bad.write_text("A # element\n6.0\ngaussian\npair\n")
+    bad.write_text("A # element\n6.0\ngaussian\nspline\n")
     with pytest.raises(mlipg.MlipgError, match="des_type"):
         mlipg.Potential(str(bad))
+    # a radial-only (pair) file cut short
+    bad.write_text("A # element\n6.0\ngaussian\npair\n")
+    with pytest.raises(mlipg.MlipgError) as e:
+        mlipg.Potential(str(bad))
+    assert e.value.code == 2
+
+
+def test_pair_potential_model(potdir):
+    """Radial-only potentials load without a GPU: the legacy enumeration gives
+    the file's coefficient count (pair-60: 60 features, 1,430 pair and 21,420
+    triple terms; pair-17: 30 features squared and cubed)."""
+    for name, d, c in (("pair-60", 60, 22910), ("pair-17", 30, 90)):
+        p = mlipg.Potential(potdir[name])
+        assert p.info["D"] == d and p.info["n_coeffs"] == c
+        assert p.elements == ["Ti", "Al"]
 
 
 @pytest.mark.skipif(os.environ.get("CUDA_VISIBLE_DEVICES") is None and

@@ -1,7 +1,7 @@
 """NVE molecular dynamics on the device against the reference's trajectories.
 
-The reference's regression runs (test/regression/gtinv-*.in: read the 32-atom
-TiAl3 cell, `fix nve`, 100 steps of 1 fs) end in `dump.atom.gtinv-*` and the
+The reference's regression runs (test/regression/{gtinv,pair}-*.in: read the
+32-atom TiAl3 cell, `fix nve`, 100 steps of 1 fs) end in `dump.atom.*` and the
 step-100 thermo line of their logs.  The FP64 path must reproduce the final
 coordinates within the reference's own tolerance (mean |dx| < 1e-4 A,
 test/regression/regression.py:9) and the printed thermo to its last printed
@@ -36,7 +36,7 @@ def run_nve(pot_path, nsteps, dt, skin=2.0, graph=True, prec=mlipg.PREC_FP64):
     return x, th
 
 
-@pytest.mark.parametrize("pot", ["gtinv-820", "gtinv-434", "gtinv-197"])
+@pytest.mark.parametrize("pot", ["gtinv-820", "gtinv-434", "gtinv-197", "pair-60", "pair-17"])
 def test_nve_100_steps_match_reference(potdir, golden, pot):
     x, th = run_nve(potdir[pot], 100, 0.001)
     ref = read_dump("dump.atom." + pot)

@@ -63,6 +63,24 @@ def test_regression_potentials_fp64(potdir, golden, pot):
     assert s.pressure(got["virial"]) == pytest.approx(gl["Press"], abs=6e-4)
 
 
+@pytest.mark.parametrize("pot", ["pair-60", "pair-17"])
+def test_pair_descriptor(potdir, golden, pot):
+    """Radial-only potentials (des_type pair, the reference's pair_style
+    mlip_pair; pair-60 has 20 radial functions and a third-order polynomial
+    of 22,910 terms): the FP64 kernel matches the oracle to 1e-10 and the
+    reference's step-0 log; every precision runs that FP64 kernel."""
+    o = Oracle(potdir[pot], threads=16)
+    s = build_system(structure("structure.lammps"), o.cutoff, skin=2.0)
+    ref = o.compute(s)
+    gl = golden["thermo_step0"][pot]
+    for prec in (mlipg.PREC_FP64, mlipg.PREC_MIXED):
+        got = mlipg.Potential(potdir[pot], prec).compute(s, vatom=True)
+        check_fp64(got, ref, s)
+        assert got["energy"] == pytest.approx(gl["E_pair"], abs=6e-6)
+        assert s.pressure(got["virial"]) == pytest.approx(gl["Press"], abs=6e-4)
+        np.testing.assert_allclose(got["vatom"].sum(0), got["virial"], rtol=1e-12, atol=1e-12)
+
+
 def test_stress_and_triclinic_fp64(potdir, golden):
     g = mlipg.Potential(potdir["gtinv-197"], mlipg.PREC_FP64)
     s = build_system(structure("structure.lammps"), g.cutoff, skin=2.0)

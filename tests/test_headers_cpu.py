@@ -43,10 +43,12 @@ def test_lammps_pair_style_compiles():
     run(["g++", "-std=c++17", "-fsyntax-only", *WARN, "-I", STUBS, "-I", INCLUDE,
          os.path.join(STYLE_DIR, "pair_mlip_gtinv_gpu.cpp")])
     # the registration block LAMMPS's style_pair.h includes
+    # (both styles, mlip_gtinv/gpu and mlip_pair/gpu, map to the one class)
     src = ('#define PAIR_CLASS\n'
-           '#define PairStyle(key, Class) static const char *style_key = #key;\n'
-           '#include "pair_mlip_gtinv_gpu.h"\n'
-           'const char *registered() { return style_key; }\n')
+           '#define CAT2(a, b) a##b\n'
+           '#define CAT(a, b) CAT2(a, b)\n'
+           '#define PairStyle(key, Class) static const char *CAT(style_key, __LINE__) = #key;\n'
+           '#include "pair_mlip_gtinv_gpu.h"\n')
     run(["g++", "-std=c++17", "-fsyntax-only", *WARN, "-I", STUBS, "-I", INCLUDE, "-I",
          STYLE_DIR, "-x", "c++", "-"], stdin=src)
 

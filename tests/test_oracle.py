@@ -11,7 +11,9 @@ from conftest import structure
 from mlipg.structures import build_system
 from oracle import Oracle
 
-CASES = [("gtinv-197", "gtinv-197"), ("gtinv-820", "gtinv-820"), ("gtinv-434", "gtinv-434")]
+CASES = [("gtinv-197", "gtinv-197"), ("gtinv-820", "gtinv-820"), ("gtinv-434", "gtinv-434"),
+         # the radial-only descriptor (pair_style mlip_pair of the reference)
+         ("pair-60", "pair-60"), ("pair-17", "pair-17")]
 
 
 @pytest.mark.parametrize("pot,log", CASES)
@@ -87,8 +89,9 @@ def test_radial_kat(tmp_path):
     np.testing.assert_allclose(fn, [0.03125, 0.5], rtol=1e-15)
 
 
-def test_finite_difference_forces_and_virial(potdir):
-    o = Oracle(potdir["gtinv-820"], threads=8)
+@pytest.mark.parametrize("pot", ["gtinv-820", "pair-17"])
+def test_finite_difference_forces_and_virial(potdir, pot):
+    o = Oracle(potdir[pot], threads=8)
     cell = structure("structure.lammps")
     s = build_system(cell, o.cutoff, skin=1.0)
     r = o.compute(s)
