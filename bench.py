@@ -79,7 +79,7 @@ POT_DESC = {
                        "model_type 3 max_p 2, 11805 coefficients ~N(0,1e-3)",
 }
 SKIN = 1.0
-PRECISIONS = {"mixed": 1, "fp64": 0, "mixed_a64": 2}   # mlipg.PREC_* values
+PRECISIONS = {"mixed": 1, "fp64": 0, "mixed_a64": 2, "fp64_native": 3}   # mlipg.PREC_* values
 PRECISION_DESC = ("mixed (MLIPG_PREC_MIXED): FP32 radial functions, Y_lm, invariant and adjoint "
                   "products; order-parameter neighbour sums in Kahan-compensated FP32 (the "
                   "mixed_a64 record times the same kernel with plain FP64 sums); the "

@@ -41,7 +41,15 @@ enum mlipg_status {
 };
 
 enum mlipg_precision {
-  MLIPG_PREC_FP64 = 0,      /* every product and sum in FP64 (plain path) */
+  MLIPG_PREC_FP64 = 0,      /* FP64 results: radial functions, Y_lm, order
+                               parameters, the polynomial, forces, energies
+                               and virial in FP64; the invariant and adjoint
+                               products in double-float arithmetic (FP32
+                               pairs, 48-bit significands, a few 2^-47
+                               relative error per operation, on the FP32
+                               pipe) with the adjoint summed in exact fixed
+                               point (order independent).  Agrees with the
+                               all-FP64 form to ~1e-13 relative. */
   MLIPG_PREC_MIXED = 1,     /* FP32 radial/Y_lm/invariant/adjoint products;
                                order-parameter neighbour sums (Kahan) and unit
                                energies (TwoSum) in compensated FP32, at FP32
@@ -51,8 +59,11 @@ enum mlipg_precision {
                                and virial accumulation in FP64.  Energy error:
                                a few FP32 ulps of sum |w_f| |d_f| over the
                                other (linear-only) features */
-  MLIPG_PREC_MIXED_A64 = 2  /* as MLIPG_PREC_MIXED, with the order-parameter
+  MLIPG_PREC_MIXED_A64 = 2, /* as MLIPG_PREC_MIXED, with the order-parameter
                                neighbour sums made with plain FP64 FMAs */
+  MLIPG_PREC_FP64_NATIVE = 3 /* every product and sum in native FP64 (the
+                               reference's arithmetic, at the FP64 pipe's
+                               rate: 1/64 of FP32 on GB300) */
 };
 
 /* Message of the last failure on this handle (h may be NULL for failures
@@ -69,7 +80,7 @@ int mlipg_create(const char* potential_path, int precision, mlipg_handle** out);
  * pair_mlip_gtinv_kokkos_impl.h:60-85) */
 int mlipg_destroy(mlipg_handle* h);
 
-/* Switches between MLIPG_PREC_FP64, MLIPG_PREC_MIXED and MLIPG_PREC_MIXED_A64. */
+/* Switches between the precisions of enum mlipg_precision. */
 int mlipg_set_precision(mlipg_handle* h, int precision);
 
 /* Elements of the potential file, their masses and the cutoff radius.

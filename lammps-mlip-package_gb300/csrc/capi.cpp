@@ -87,7 +87,9 @@ struct mlipg_handle {
   // model tables on the device
   DevBuf d_terms, d_units, d_unit_off, d_nl, d_nl_off, d_poly, d_poly_off, d_wlin, d_radial;
   DevBuf d_terms_f;   // the same terms with the coefficient as FP32 (mixed path)
+  DevBuf d_terms_df;  // ... as a (high, low) FP32 pair (double-float path)
   DevBuf d_iunits, d_iunit_off, d_tuples, d_wlin_f, d_phase, d_adj_base, d_adj_off, d_adj;
+  DevBuf d_wlin_df;
   DevBuf d_radial_rec;   // FP64 radial recurrence constants (common beta), or empty
   DevBuf d_pair_terms, d_pair_term_off, d_pair_adj, d_pair_adj_off, d_type_pairs;
   double rec_q = 0.0;
@@ -203,6 +205,15 @@ static int upload_model(mlipg_handle* h) {
       }
     }
     CK(upload(h->d_terms_f, tf, s), "upload FP32 terms");
+    // double-float coefficients: high word = FP32 rounding, low word = the
+    // FP32 rounding of the rest (the 8-byte field's two 4-byte halves)
+    std::vector<DeviceTerm> td(M.cterms);
+    for (auto& t : td) {
+      const float hi = to_f32(t.c), lo = to_f32(t.c - (double)hi);
+      std::memcpy(reinterpret_cast<char*>(&t.c), &hi, sizeof hi);
+      std::memcpy(reinterpret_cast<char*>(&t.c) + 4, &lo, sizeof lo);
+    }
+    CK(upload(h->d_terms_df, td, s), "upload double-float terms");
   }
   CK(upload(h->d_units, units, s), "upload units");
   CK(upload(h->d_iunits, iunits, s), "upload batched units");
@@ -221,6 +232,12 @@ static int upload_model(mlipg_handle* h) {
     std::vector<float> wf(M.w_lin.size());
     for (size_t k = 0; k < wf.size(); ++k) wf[k] = to_f32(M.w_lin[k]);
     CK(upload(h->d_wlin_f, wf, s), "upload linear weights (FP32)");
+    std::vector<float> wd(2 * M.w_lin.size());
+    for (size_t k = 0; k < M.w_lin.size(); ++k) {
+      wd[2 * k] = to_f32(M.w_lin[k]);
+      wd[2 * k + 1] = to_f32(M.w_lin[k] - (double)wd[2 * k]);
+    }
+    CK(upload(h->d_wlin_df, wd, s), "upload linear weights (double-float)");
   }
   CK(upload(h->d_radial, radial, s), "upload radial parameters");
   if (M.pot.pair) {
@@ -270,7 +287,7 @@ const char* mlipg_last_error(const mlipg_handle* h) {
 int mlipg_create(const char* path, int precision, mlipg_handle** out) {
   if (!out || !path) return fail(nullptr, MLIPG_EINVAL, "mlipg_create: null argument");
   *out = nullptr;
-  if (precision < MLIPG_PREC_FP64 || precision > MLIPG_PREC_MIXED_A64)
+  if (precision < MLIPG_PREC_FP64 || precision > MLIPG_PREC_FP64_NATIVE)
     return fail(nullptr, MLIPG_EINVAL, "unknown precision %d", precision);
   mlipg_handle* h = new mlipg_handle();
   h->precision = precision;
@@ -326,7 +343,8 @@ int mlipg_destroy(mlipg_handle* h) {
   mlipg_internal_features_release(h);
   DevBuf* bufs[] = {&h->d_adj_base, &h->d_adj_off, &h->d_adj,
                     &h->d_iunits, &h->d_iunit_off, &h->d_tuples, &h->d_wlin_f, &h->d_phase,
-                    &h->d_terms, &h->d_terms_f, &h->d_units, &h->d_unit_off, &h->d_nl,
+                    &h->d_terms, &h->d_terms_f, &h->d_terms_df, &h->d_wlin_df,
+                    &h->d_units, &h->d_unit_off, &h->d_nl,
                     &h->d_nl_off,
                     &h->d_poly, &h->d_poly_off, &h->d_wlin, &h->d_radial, &h->d_radial_rec,
                     &h->d_pair_terms, &h->d_pair_term_off, &h->d_pair_adj, &h->d_pair_adj_off,
@@ -347,7 +365,7 @@ int mlipg_destroy(mlipg_handle* h) {
 
 int mlipg_set_precision(mlipg_handle* h, int precision) {
   if (!h) return fail(nullptr, MLIPG_EINVAL, "null handle");
-  if (precision < MLIPG_PREC_FP64 || precision > MLIPG_PREC_MIXED_A64)
+  if (precision < MLIPG_PREC_FP64 || precision > MLIPG_PREC_FP64_NATIVE)
     return fail(h, MLIPG_EINVAL, "unknown precision %d", precision);
   h->precision = precision;
   return MLIPG_OK;
@@ -428,6 +446,22 @@ static int effective_nb_cap(int nb_cap) {
   return std::max(32, std::min(kNbCapMax, (nb_cap + 31) / 32 * 32));
 }
 
+static bool is_mixed(int precision) {
+  return precision == MLIPG_PREC_MIXED || precision == MLIPG_PREC_MIXED_A64;
+}
+
+// Kernel instantiation of the handle's precision: MLIPG_PREC_FP64 runs the
+// double-float invariant/adjoint phase when its fixed-point bound exists and
+// its shared memory fits, else the all-FP64 kernel.
+static int kernel_variant(const mlipg_handle* h, int nb_cap) {
+  const Model& M = h->model;
+  if (is_mixed(h->precision)) return kVariantF32;
+  if (h->precision == MLIPG_PREC_FP64 && M.g_bound_df > 0 &&
+      fused_smem_bytes(kVariantF64DF, M.T, M.L, nb_cap, std::max(M.max_nl, 1), 0) <= 227 * 1024)
+    return kVariantF64DF;
+  return kVariantF64;
+}
+
 // Shared-memory bytes and resident CTAs per SM of the fused kernel for this
 // handle's model, precision and neighbour capacity.
 static int kernel_shape(mlipg_handle* h, int nb_cap, size_t* smem, int* bps) {
@@ -439,14 +473,15 @@ static int kernel_shape(mlipg_handle* h, int nb_cap, size_t* smem, int* bps) {
     if (*bps < 1) return fail(h, MLIPG_ENOTSUP, "pair kernel cannot be resident (smem %zu)", *smem);
     return MLIPG_OK;
   }
-  const bool fp64 = h->precision == MLIPG_PREC_FP64;
-  *smem = fused_smem_bytes(fp64, M.T, M.L, nb_cap, std::max(M.max_nl, 1), fp64 ? 0 : M.lh64);
+  const int var = kernel_variant(h, nb_cap);
+  *smem = fused_smem_bytes(var, M.T, M.L, nb_cap, std::max(M.max_nl, 1),
+                           var == kVariantF32 ? M.lh64 : 0);
   if (*smem > 227 * 1024)
     return fail(h, MLIPG_ENOTSUP,
                 "model needs %zu bytes of shared memory per CTA (limit 232448): "
                 "reduce elements, max_l or radial functions",
                 *smem);
-  *bps = fused_max_blocks_per_sm(fp64, M.L, *smem);
+  *bps = fused_max_blocks_per_sm(var, M.L, *smem);
   if (*bps < 1) return fail(h, MLIPG_ENOTSUP, "fused kernel cannot be resident (smem %zu)", *smem);
   if (M.tiling.ctas_per_sm > 0) *bps = std::min(*bps, M.tiling.ctas_per_sm);
   return MLIPG_OK;
@@ -473,8 +508,8 @@ static int launch_eval(mlipg_handle* h, int ncenters, const double4* x4, const i
                        double* eatom, double* vatom, double* out8, double* partials,
                        int partial_slots, int* status, bool timed) {
   const Model& M = h->model;
-  const bool fp64 = h->precision == MLIPG_PREC_FP64;
   nb_cap = effective_nb_cap(nb_cap);
+  const int var = kernel_variant(h, nb_cap);
   size_t smem = 0;
   int bps = 0;
   int rc = kernel_shape(h, nb_cap, &smem, &bps);
@@ -495,7 +530,9 @@ static int launch_eval(mlipg_handle* h, int ncenters, const double4* x4, const i
   a.center_cell = center_cell;
   a.fold = fold;
   a.ncenters = ncenters;
-  a.terms = (fp64 ? h->d_terms : h->d_terms_f).as<DeviceTerm>();
+  a.terms = (var == kVariantF32 ? h->d_terms_f
+                                 : (var == kVariantF64DF ? h->d_terms_df : h->d_terms))
+                .as<DeviceTerm>();
   a.terms64 = h->d_terms.as<DeviceTerm>();
   a.units = h->d_units.as<DeviceUnit>();
   a.unit_off = h->d_unit_off.as<int>();
@@ -511,6 +548,7 @@ static int launch_eval(mlipg_handle* h, int ncenters, const double4* x4, const i
   a.adj = h->d_adj.as<DeviceAdj>();
   a.w_lin = h->d_wlin.as<double>();
   a.w_lin_f = h->d_wlin_f.as<float>();
+  a.w_lin_df = h->d_wlin_df.as<float2>();
   a.phase_clocks = h->profiling ? h->d_phase.as<unsigned long long>() : nullptr;
   a.radial = h->d_radial.as<double>();
   a.pair_terms = h->d_pair_terms.as<DevicePairTerm>();
@@ -528,10 +566,10 @@ static int launch_eval(mlipg_handle* h, int ncenters, const double4* x4, const i
   a.nb_cap = nb_cap;
   a.nl_cap = std::max(M.max_nl, 1);
   a.rc = M.pot.cutoff;
-  a.g_bound = (float)M.g_bound;
+  a.g_bound = (float)(var == kVariantF64DF ? M.g_bound_df : M.g_bound);
   a.unit_dyn = M.tiling.warp_order == 2 ? 1 : 0;
   a.sum64 = h->precision == MLIPG_PREC_MIXED_A64 ? 1 : 0;
-  a.lh64 = fp64 ? 0 : M.lh64;
+  a.lh64 = var == kVariantF32 ? M.lh64 : 0;
   a.f = f;
   a.eatom = eatom;
   a.vatom = vatom;
@@ -552,7 +590,7 @@ static int launch_eval(mlipg_handle* h, int ncenters, const double4* x4, const i
   if (ncenters > 0 && M.pot.pair) {
     CK(launch_pair(a, grid, smem, h->stream), "pair kernel launch");
   } else if (ncenters > 0) {
-    CK(launch_fused(fp64, M.L, a, grid, smem, h->stream), "fused kernel launch");
+    CK(launch_fused(var, M.L, a, grid, smem, h->stream), "fused kernel launch");
   } else {
     CK(cudaMemsetAsync(partials, 0, 8 * sizeof(double), h->stream), "memset partials");
   }
@@ -872,11 +910,11 @@ extern "C" int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4,
     if (nreport) *nreport = 0;
     return MLIPG_OK;
   }
-  const bool fp64 = h->precision == MLIPG_PREC_FP64;
   const int cap = effective_nb_cap(nb_cap);
-  const size_t smem =
-      fused_smem_bytes(fp64, M.T, M.L, cap, std::max(M.max_nl, 1), fp64 ? 0 : M.lh64);
-  const int bps_max = std::max(1, fused_max_blocks_per_sm(fp64, M.L, smem));
+  const int var = kernel_variant(h, cap);
+  const size_t smem = fused_smem_bytes(var, M.T, M.L, cap, std::max(M.max_nl, 1),
+                                       var == kVariantF32 ? M.lh64 : 0);
+  const int bps_max = std::max(1, fused_max_blocks_per_sm(var, M.L, smem));
   // a sample of 16 centres per resident CTA keeps each candidate short
   const int sample = std::min(ncenters, 16 * bps_max * h->num_sms);
   const Tiling start = M.tiling;

@@ -26,7 +26,10 @@
 // neighbour's own evaluation (identical to the reference's j<i / ghost
 // split up to summation order).
 //
-// Required macros: MLIPG_REAL (float|double), MLIPG_TAG (f32|f64); with
+// Required macros: MLIPG_REAL (float|double), MLIPG_TAG (f32|f64|f64df);
+// MLIPG_DF (with MLIPG_REAL double) runs P5's products in double-float
+// arithmetic (dfloat.cuh) on the FP32 pipe, with the adjoint accumulated in
+// exact four-word fixed point; every other phase stays FP64.  With
 // MLIPG_NO_FUSED defined, only the device helpers (spherical harmonics,
 // radial basis, displacements) and init_constants are compiled.
 
@@ -35,6 +38,7 @@
 #include <cstdint>
 #include <type_traits>
 
+#include "dfloat.cuh"
 #include "kernels.cuh"
 
 #define MLIPG_CAT2(a, b) a##b
@@ -47,7 +51,23 @@ using R = MLIPG_REAL;
 template <typename T> struct Cx;
 template <> struct Cx<float> { using type = float2; };
 template <> struct Cx<double> { using type = double2; };
+template <> struct Cx<DF> { using type = DFc; };
 using Rc = Cx<R>::type;
+#ifdef MLIPG_DF
+constexpr bool kDF = true;
+#else
+constexpr bool kDF = false;
+#endif
+// P5's arithmetic type, its complex type and the adjoint's storage word:
+// FP32 (fixed point in int32 pairs), FP64 (FP64 atomics) or double-float
+// (fixed point in four int32 words)
+using P = std::conditional_t<kDF, DF, R>;
+using Pc = Cx<P>::type;
+using PG = std::conditional_t<kDF, int, R>;
+// the adjoint is accumulated in fixed point (and range-checked)
+constexpr bool kFixG = sizeof(R) == 4 || kDF;
+// 4-byte words of adjoint storage per complex entry
+constexpr int kGWords = kDF ? 8 : 4;
 // resident CTAs per SM the register allocation targets: two for FP32
 // products (shared memory allows two), one for FP64 (its shared memory
 // allows only one, so registers are not capped)
@@ -344,6 +364,11 @@ __device__ __forceinline__ void merge_unit_energy(ESumF& es, double&, const ESum
   two_sum_acc(es.s, es.c, u.s);
 }
 __device__ __forceinline__ void merge_unit_energy(ESumF&, double& ed, double u) { ed += u; }
+// double-float path: a double-float sum per unit, added to the FP64 energy
+__device__ __forceinline__ void eadd(DF& e, DF v) { e += v; }
+__device__ __forceinline__ void merge_unit_energy(ESumF&, double& ed, const DF& u) {
+  ed += df_to_double(u);
+}
 
 // Sum over the warp's lanes of one unit's energy, identical on every lane.
 // FP64: a butterfly of FP64 adds.  Mixed: a butterfly of TwoSum steps in FP32
@@ -368,6 +393,25 @@ __device__ __forceinline__ double warp_energy(ESumF e) {
   }
   return (double)s + (double)c;
 }
+__device__ __forceinline__ double warp_energy(DF e) { return warp_energy(df_to_double(e)); }
+
+// sum of the two half-warps' partial invariants of one unit at channel n
+__device__ __forceinline__ double half_pair_sum(float v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 16);
+  return (double)v;
+}
+__device__ __forceinline__ double half_pair_sum(double v) {
+  return v + __shfl_xor_sync(0xffffffffu, v, 16);
+}
+__device__ __forceinline__ double half_pair_sum(DF v) { return half_pair_sum(df_to_double(v)); }
+
+// a statically dealt unit's energy accumulator
+using EU = std::conditional_t<sizeof(R) == 4, ESumF, std::conditional_t<kDF, DF, double>>;
+// an FP64 weight in P5's arithmetic type
+__device__ __forceinline__ float to_p_as(double v, float*) { return (float)v; }
+__device__ __forceinline__ double to_p_as(double v, double*) { return v; }
+__device__ __forceinline__ DF to_p_as(double v, DF*) { return df_from_double(v); }
+__device__ __forceinline__ P to_p(double v) { return to_p_as(v, (P*)nullptr); }
 
 // four consecutive values from 16-byte aligned shared memory
 __device__ __forceinline__ void load4(const float* p, float* v) {
@@ -434,12 +478,18 @@ __device__ __forceinline__ void pair_disp(const KernelArgs& A, int c, int k, con
   }
 }
 
-// One coupling unit for all n: warp halves take alternate terms.
 // Coupling coefficient of a term record: FP64 in the FP64 path's table; the
-// mixed path's table holds it as FP32 in the low word (no conversion per term).
-__device__ __forceinline__ R term_coeff(const int4& raw) {
-  if constexpr (sizeof(R) == 4) return __int_as_float(raw.x);
-  else return __hiloint2double(raw.y, raw.x);
+// mixed path's table holds it as FP32 in the low word, the double-float
+// table as (high, low) FP32 words (no conversion per term).
+template <class V> __device__ __forceinline__ V term_coeff(const int4& raw);
+template <> __device__ __forceinline__ float term_coeff<float>(const int4& raw) {
+  return __int_as_float(raw.x);
+}
+template <> __device__ __forceinline__ double term_coeff<double>(const int4& raw) {
+  return __hiloint2double(raw.y, raw.x);
+}
+template <> __device__ __forceinline__ DF term_coeff<DF>(const int4& raw) {
+  return DF(__int_as_float(raw.x), __int_as_float(raw.y));
 }
 
 // Sum of the batched units' energies taken from a shared counter: the two
@@ -455,55 +505,91 @@ __device__ __forceinline__ double unit_energy(const int* misc) {
 // Each flush is scaled by 2^e (e adapted per centre element) and split
 // exactly into a high part, a multiple of 2^16, and a low part of at most
 // 2^15 (both rounded by the exact magic-number add), which go to two int32
-// arrays (the low-part array follows the high parts of re and im); no carries are needed because the host
-// bounds the flushes per entry.  Sums are exact and order independent; the
-// centre's largest |scaled flush| is tracked so that out-of-range flushes are
-// detected (the invariant phase is then redone at a smaller scale).
-struct GFix {
-  R scale;     // 2^e
-  R vmax;      // largest |scaled flush| of this thread
+// arrays (the low-part array follows the high parts of re and im); no
+// carries are needed because the host bounds the flushes per entry.
+// Double-float path: four words, multiples of 2^48, 2^32, 2^16 and 1.
+// Sums are exact and order independent; the centre's largest |scaled flush|
+// is tracked so that out-of-range flushes are detected (the invariant phase
+// is then redone at a smaller scale).
+template <class V> struct GFixT {
+  V scale;     // 2^e (1 in FP64)
+  V vmax;      // largest |scaled flush| of this thread
 };
-// y: the flush already multiplied by g.scale (1 in FP64); lo: element offset
-// of the low-part array (2 x the imaginary offset)
-__device__ __forceinline__ void gput(R* p, R y, GFix& g, int lo) {
-  if constexpr (sizeof(R) == 4) {
-    g.vmax = fmaxf(g.vmax, fabsf(y));
-    const float th = fmaf(y, 1.0f / 65536.0f, 12582912.0f);   // rint(y / 2^16) + 1.5 * 2^23
-    const float yl = fmaf(-(th - 12582912.0f), 65536.0f, y);  // y - hi * 2^16, exact
-    atomicAdd(reinterpret_cast<int*>(p), __float_as_int(th) - 0x4B400000);
-    atomicAdd(reinterpret_cast<int*>(p) + lo, __float2int_rn(yl));   // |yl| <= 2^15 + 1/2
-  } else {
-    atomicAdd(p, y);
-  }
+template <> struct GFixT<DF> {
+  float scale;
+  float vmax;
+};
+__device__ __forceinline__ float gscale(float c, const GFixT<float>& g) { return c * g.scale; }
+__device__ __forceinline__ double gscale(double c, const GFixT<double>& g) { return c * g.scale; }
+__device__ __forceinline__ DF gscale(DF c, const GFixT<DF>& g) { return df_scale(c, g.scale); }
+
+// y: the flush already multiplied by g.scale; lo: word offset of the next
+// lower word array (2 x the imaginary offset)
+__device__ __forceinline__ void gput(float* p, float y, GFixT<float>& g, int lo) {
+  g.vmax = fmaxf(g.vmax, fabsf(y));
+  const float th = fmaf(y, 1.0f / 65536.0f, 12582912.0f);   // rint(y / 2^16) + 1.5 * 2^23
+  const float yl = fmaf(-(th - 12582912.0f), 65536.0f, y);  // y - hi * 2^16, exact
+  atomicAdd(reinterpret_cast<int*>(p), __float_as_int(th) - 0x4B400000);
+  atomicAdd(reinterpret_cast<int*>(p) + lo, __float2int_rn(yl));   // |yl| <= 2^15 + 1/2
+}
+__device__ __forceinline__ void gput(double* p, double y, GFixT<double>&, int) {
+  atomicAdd(p, y);
+}
+// Double-float flush y = yh + yl (|yh| below the host's bound, at most 2^70):
+// yh = t3 2^48 + t2 2^32 + t1 2^16 + r0 and yl = u2 2^32 + u1 2^16 + q0
+// exactly (magic-number roundings; every remainder is representable), then
+// the words t3, t2 + u2, t1 + u1 and rint(r0 + q0) (|.| <= 2^16 + 1) are
+// added: 64 bits below the largest flush, so an entry 2^16 times smaller
+// than the centre's largest flush still keeps 48 bits.
+__device__ __forceinline__ int magic_int(float t) { return __float_as_int(t) - 0x4B400000; }
+__device__ __forceinline__ void gput(int* p, DF y, GFixT<DF>& g, int lo) {
+  constexpr float kMagic = 12582912.0f;   // 1.5 * 2^23
+  g.vmax = fmaxf(g.vmax, fabsf(y.h));
+  const float th3 = __fmaf_rn(y.h, 0x1p-48f, kMagic);
+  const float r2 = __fmaf_rn(-__fsub_rn(th3, kMagic), 0x1p48f, y.h);   // |r2| <= 2^47
+  const float th2 = __fmaf_rn(r2, 0x1p-32f, kMagic);
+  const float r1 = __fmaf_rn(-__fsub_rn(th2, kMagic), 0x1p32f, r2);    // |r1| <= 2^31
+  const float th1 = __fmaf_rn(r1, 0x1p-16f, kMagic);
+  const float r0 = __fmaf_rn(-__fsub_rn(th1, kMagic), 65536.0f, r1);   // |r0| <= 2^15
+  const float sh2 = __fmaf_rn(y.l, 0x1p-32f, kMagic);
+  const float q1 = __fmaf_rn(-__fsub_rn(sh2, kMagic), 0x1p32f, y.l);   // |q1| <= 2^31
+  const float sh1 = __fmaf_rn(q1, 0x1p-16f, kMagic);
+  const float q0 = __fmaf_rn(-__fsub_rn(sh1, kMagic), 65536.0f, q1);   // |q0| <= 2^15
+  const float t0 = __fadd_rn(__fadd_rn(r0, q0), kMagic);
+  atomicAdd(p, magic_int(th3));
+  atomicAdd(p + lo, magic_int(th2) + magic_int(sh2));
+  atomicAdd(p + 2 * lo, magic_int(th1) + magic_int(sh1));
+  atomicAdd(p + 3 * lo, magic_int(t0));
 }
 
-template <int Q, bool WITH_G, int Lh>
+template <class V, int Q, bool WITH_G, int Lh, class GT>
 __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* __restrict__ terms,
-                                         const Rc* sa, R* sg, int gim, GFix& gf, int n,
-                                         int half, bool act, R H, R& dsum) {
+                                         const typename Cx<V>::type* sa, GT* sg, int gim,
+                                         GFixT<V>& gf, int n, int half, bool act, V H, V& dsum) {
+  using Vc = typename Cx<V>::type;
   int off[Q];
 #pragma unroll
   for (int p = 0; p < Q; ++p) off[p] = (int)u.s[p] * Lh * kNPad + n;
   const int kend = u.term0 + u.nterm;
   for (int k = u.term0 + half; k < kend; k += 2) {
     const int4 raw = __ldg(reinterpret_cast<const int4*>(terms + k));
-    const R c = term_coeff(raw);
+    const V c = term_coeff<V>(raw);
     const unsigned lw = (unsigned)raw.z, hw = (unsigned)raw.w;
     const unsigned code = hw >> 16;
     int lmh[Q];
-    R ar[Q], ai[Q];
+    V ar[Q], ai[Q];
 #pragma unroll
     for (int p = 0; p < Q; ++p) {
       lmh[p] = p < 4 ? (int)((lw >> (8 * p)) & 255u) : (int)((hw >> (8 * (p - 4))) & 255u);
-      const Rc v = sa[off[p] + lmh[p] * kNPad];
+      const Vc v = sa[off[p] + lmh[p] * kNPad];
       const unsigned cd = (code >> (2 * p)) & 3u;
       ar[p] = v.x;
       ai[p] = (cd == (unsigned)kSlotConj) ? -v.y : v.y;
     }
     const bool self = (code >> 12) & 1u;
     // prefix products pr[p] = prod_{p' < p} a~, suffix su[p] = prod_{p' > p} a~
-    R prr[Q], pri[Q], sur[Q], sui[Q];
-    prr[0] = R(1); pri[0] = R(0);
+    V prr[Q], pri[Q], sur[Q], sui[Q];
+    prr[0] = V(1); pri[0] = V(0);
 #pragma unroll
     for (int p = 1; p < Q; ++p) {
       if (p == 1) { prr[1] = ar[0]; pri[1] = ai[0]; }
@@ -512,7 +598,7 @@ __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* 
         pri[p] = prr[p - 1] * ai[p - 1] + pri[p - 1] * ar[p - 1];
       }
     }
-    sur[Q - 1] = R(1); sui[Q - 1] = R(0);
+    sur[Q - 1] = V(1); sui[Q - 1] = V(0);
 #pragma unroll
     for (int p = Q - 2; p >= 0; --p) {
       if (p == Q - 2) { sur[p] = ar[Q - 1]; sui[p] = ai[Q - 1]; }
@@ -522,13 +608,13 @@ __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* 
       }
     }
     // full product real part
-    const R full = prr[Q - 1] * ar[Q - 1] - pri[Q - 1] * ai[Q - 1];
-    dsum += (self ? c : R(2) * c) * full;
+    const V full = prr[Q - 1] * ar[Q - 1] - pri[Q - 1] * ai[Q - 1];
+    dsum += (self ? c : V(2) * c) * full;
     if (WITH_G) {
-      const R cc = c * H;
+      const V cc = c * H;
 #pragma unroll
       for (int p = 0; p < Q; ++p) {
-        R Pr, Pi;
+        V Pr, Pi;
         if (p == 0) { Pr = sur[0]; Pi = sui[0]; }
         else if (p == Q - 1) { Pr = prr[Q - 1]; Pi = pri[Q - 1]; }
         else {
@@ -536,13 +622,13 @@ __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* 
           Pi = prr[p] * sui[p] + pri[p] * sur[p];
         }
         const unsigned cd = (code >> (2 * p)) & 3u;
-        const R kr = (cd == (unsigned)kSlotMZero) ? R(2) : R(1);
-        const R ki = (cd == 0u) ? R(1) : (cd == 1u ? R(-1) : R(0));
+        const V kr = (cd == (unsigned)kSlotMZero) ? V(2) : V(1);
+        const V ki = (cd == 0u) ? V(1) : (cd == 1u ? V(-1) : V(0));
         // unconditional: lanes n >= F and unused imaginary parts add exact
         // zeros (to padding entries / entries nothing reads), which keeps the
         // flush free of divergent branches
-        R* gp = sg + off[p] + lmh[p] * kNPad;
-        const R cs = cc * gf.scale;
+        GT* gp = sg + off[p] + lmh[p] * kNPad;
+        const V cs = gscale(cc, gf);
         gput(gp, cs * kr * Pr, gf, 2 * gim);
         gput(gp + gim, cs * ki * Pi, gf, 2 * gim);
       }
@@ -550,11 +636,20 @@ __device__ __forceinline__ void run_unit(const DeviceUnit& u, const DeviceTerm* 
   }
 }
 
-// linear weights in the arithmetic precision of the products
-__device__ __forceinline__ const float* wlin_pick(const double*, const float* f, float*) { return f; }
-__device__ __forceinline__ const double* wlin_pick(const double* d, const float*, double*) { return d; }
-__device__ __forceinline__ const R* wlin_table(const KernelArgs& A) {
-  return wlin_pick(A.w_lin, A.w_lin_f, (R*)nullptr);
+// linear weights in P5's arithmetic type
+__device__ __forceinline__ const float* wlin_pick(const KernelArgs& A, float*) { return A.w_lin_f; }
+__device__ __forceinline__ const double* wlin_pick(const KernelArgs& A, double*) { return A.w_lin; }
+__device__ __forceinline__ const DF* wlin_pick(const KernelArgs& A, DF*) {
+  return reinterpret_cast<const DF*>(A.w_lin_df);
+}
+__device__ __forceinline__ const P* wlin_table(const KernelArgs& A) {
+  return wlin_pick(A, (P*)nullptr);
+}
+__device__ __forceinline__ float ldg_v(const float* p) { return __ldg(p); }
+__device__ __forceinline__ double ldg_v(const double* p) { return __ldg(p); }
+__device__ __forceinline__ DF ldg_v(const DF* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return DF(v.x, v.y);
 }
 
 // Direct form for up to two elements and orders <= 3: every tuple of the
@@ -568,24 +663,26 @@ __device__ __forceinline__ const R* wlin_table(const KernelArgs& A) {
 // tuple or an idle lane).  Both loads are issued unconditionally from clamped
 // rows (row 0 always exists; the nonlinear row n < 16 lies inside shared
 // memory) so the unrolled setup of a unit issues all its loads at once.
-__device__ __forceinline__ R tuple_weight(int2 e, const R* __restrict__ wlin, const R* hnl, int n,
+template <class V>
+__device__ __forceinline__ V tuple_weight(int2 e, const V* __restrict__ wlin, const V* hnl, int n,
                                           bool act) {
-  const R w = __ldg(wlin + (size_t)max(e.x, 0) * kNPad + n);
-  const R hn = hnl[max(e.y, 0) * kNPad + n];
-  const R h = e.y >= 0 ? w + hn : w;
-  return (act && e.x >= 0) ? h : R(0);
+  const V w = ldg_v(wlin + (size_t)max(e.x, 0) * kNPad + n);
+  const V hn = hnl[max(e.y, 0) * kNPad + n];
+  const V h = e.y >= 0 ? w + hn : w;
+  return (act && e.x >= 0) ? h : V(0);
 }
 
-template <int Q, int TT, int Lh, class EA>
+template <class V, int Q, int TT, int Lh, class EA, class GT>
 __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
-                                        const R* __restrict__ wlin, const R* hnl,
-                                        const Rc* sa, R* sg, int gim, GFix& gf, int n,
-                                        int half, bool act, EA& eacc) {
+                                        const V* __restrict__ wlin, const V* hnl,
+                                        const typename Cx<V>::type* sa, GT* sg, int gim,
+                                        GFixT<V>& gf, int n, int half, bool act, EA& eacc) {
+  using Vc = typename Cx<V>::type;
   constexpr int N0 = TT;                                  // elements of slot 0
   constexpr int NT = (Q == 1) ? N0 : (Q == 2 ? N0 * TT : N0 * TT * TT);
   constexpr int s0base = 0;
-  R H[NT];
+  V H[NT];
 #pragma unroll
   for (int j = 0; j < NT; ++j) {
     const int2 e = __ldg(reinterpret_cast<const int2*>(tups + u.tup + j));
@@ -594,19 +691,19 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
   // Energy: sum_j H_j d_j of this unit's tuples, formed per term from the
   // last slot's adjoint partial (sum_j H_j Pi_j = sum_s g_last[s] a_last[s]);
   // the nonlinear part sum hnl d of H is subtracted once per centre.
-  R eu = R(0);
+  V eu = V(0);
   constexpr int es = Lh * kNPad;   // element stride in the a / G arrays
   constexpr int kIm = TT * es, kLo = 2 * kIm;   // imaginary / low-part offsets (T == TT)
   const int kend = u.term0 + u.nterm;
   for (int k = u.term0 + half; k < kend; k += 2) {
     const int4 raw = __ldg(reinterpret_cast<const int4*>(terms + k));
-    const R c = term_coeff(raw);
+    const V c = term_coeff<V>(raw);
     const unsigned lw = (unsigned)raw.z, code = ((unsigned)raw.w) >> 16;
     const bool self = (code >> 12) & 1u;
-    const R ce = self ? c : R(2) * c;
+    const V ce = self ? c : V(2) * c;
     int lo[Q];
-    R ar0[N0], ai0[N0];
-    R ar[Q][TT], ai[Q][TT];    // slots >= 1 (slot 0 uses ar0 / ai0)
+    V ar0[N0], ai0[N0];
+    V ar[Q][TT], ai[Q][TT];    // slots >= 1 (slot 0 uses ar0 / ai0)
 #pragma unroll
     for (int p = 0; p < Q; ++p) {
       lo[p] = (int)((lw >> (8 * p)) & 255u) * kNPad + n;
@@ -614,28 +711,28 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
       if (p == 0) {
 #pragma unroll
         for (int s = 0; s < N0; ++s) {
-          const Rc v = sa[(s0base + s) * es + lo[0]];
+          const Vc v = sa[(s0base + s) * es + lo[0]];
           ar0[s] = v.x;
           ai0[s] = cj ? -v.y : v.y;
         }
       } else {
 #pragma unroll
         for (int s = 0; s < TT; ++s) {
-          const Rc v = sa[s * es + lo[p]];
+          const Vc v = sa[s * es + lo[p]];
           ar[p][s] = v.x;
           ai[p][s] = cj ? -v.y : v.y;
         }
       }
     }
-    R g0r[N0], g0i[N0], gr[Q][TT], gi[Q][TT];
+    V g0r[N0], g0i[N0], gr[Q][TT], gi[Q][TT];
 #pragma unroll
-    for (int s = 0; s < N0; ++s) { g0r[s] = R(0); g0i[s] = R(0); }
+    for (int s = 0; s < N0; ++s) { g0r[s] = V(0); g0i[s] = V(0); }
 #pragma unroll
     for (int p = 0; p < Q; ++p)
 #pragma unroll
-      for (int s = 0; s < TT; ++s) { gr[p][s] = R(0); gi[p][s] = R(0); }
+      for (int s = 0; s < TT; ++s) { gr[p][s] = V(0); gi[p][s] = V(0); }
     if (Q == 1) {
-      R et = R(0);
+      V et = V(0);
 #pragma unroll
       for (int s0 = 0; s0 < N0; ++s0) {
         g0r[s0] += H[s0];
@@ -648,17 +745,17 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
 #pragma unroll
         for (int s1 = 0; s1 < TT; ++s1) {
           const int j = s0 * TT + s1;
-          const R h = H[j];
+          const V h = H[j];
           g0r[s0] += h * ar[1][s1]; g0i[s0] += h * ai[1][s1];
           gr[1][s1] += h * ar0[s0]; gi[1][s1] += h * ai0[s0];
         }
-      R et = R(0);
+      V et = V(0);
 #pragma unroll
       for (int s1 = 0; s1 < TT; ++s1) et += gr[1][s1] * ar[1][s1] - gi[1][s1] * ai[1][s1];
       eu += ce * et;
     } else {
       // b12[s1][s2] = a1 a2 (adjoint of slot 0)
-      R b12r[TT][TT], b12i[TT][TT];
+      V b12r[TT][TT], b12i[TT][TT];
 #pragma unroll
       for (int x = 0; x < TT; ++x)
 #pragma unroll
@@ -668,7 +765,7 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
         }
 #pragma unroll
       for (int s0 = 0; s0 < N0; ++s0) {
-        R b02r[TT], b02i[TT];   // a0 a2 (adjoint of slot 1)
+        V b02r[TT], b02i[TT];   // a0 a2 (adjoint of slot 1)
 #pragma unroll
         for (int y = 0; y < TT; ++y) {
           b02r[y] = ar0[s0] * ar[2][y] - ai0[s0] * ai[2][y];
@@ -676,19 +773,19 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
         }
 #pragma unroll
         for (int s1 = 0; s1 < TT; ++s1) {
-          const R pr = ar0[s0] * ar[1][s1] - ai0[s0] * ai[1][s1];   // a0 a1 (slot 2)
-          const R pi = ar0[s0] * ai[1][s1] + ai0[s0] * ar[1][s1];
+          const V pr = ar0[s0] * ar[1][s1] - ai0[s0] * ai[1][s1];   // a0 a1 (slot 2)
+          const V pi = ar0[s0] * ai[1][s1] + ai0[s0] * ar[1][s1];
 #pragma unroll
           for (int s2 = 0; s2 < TT; ++s2) {
             const int j = (s0 * TT + s1) * TT + s2;
-            const R h = H[j];
+            const V h = H[j];
             g0r[s0] += h * b12r[s1][s2]; g0i[s0] += h * b12i[s1][s2];
             gr[1][s1] += h * b02r[s2];   gi[1][s1] += h * b02i[s2];
             gr[2][s2] += h * pr;         gi[2][s2] += h * pi;
           }
         }
       }
-      R et = R(0);
+      V et = V(0);
 #pragma unroll
       for (int s2 = 0; s2 < TT; ++s2) et += gr[2][s2] * ar[2][s2] - gi[2][s2] * ai[2][s2];
       eu += ce * et;
@@ -697,20 +794,20 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
 #pragma unroll
     for (int p = 0; p < Q; ++p) {
       const unsigned cd = (code >> (2 * p)) & 3u;
-      const R cs = c * gf.scale;
-      const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * cs : cs;
-      const R ki = (cd == 0u) ? cs : (cd == 1u ? -cs : R(0));
+      const V cs = gscale(c, gf);
+      const V kr = (cd == (unsigned)kSlotMZero) ? V(2) * cs : cs;
+      const V ki = (cd == 0u) ? cs : (cd == 1u ? -cs : V(0));
       if (p == 0) {
 #pragma unroll
         for (int s = 0; s < N0; ++s) {
-          R* gp = sg + (s0base + s) * es + lo[0];
+          GT* gp = sg + (s0base + s) * es + lo[0];
           gput(gp, kr * g0r[s], gf, kLo);
           gput(gp + kIm, ki * g0i[s], gf, kLo);
         }
       } else {
 #pragma unroll
         for (int s = 0; s < TT; ++s) {
-          R* gp = sg + s * es + lo[p];
+          GT* gp = sg + s * es + lo[p];
           gput(gp, kr * gr[p][s], gf, kLo);
           gput(gp + kIm, ki * gi[p][s], gf, kLo);
         }
@@ -723,11 +820,12 @@ __device__ __forceinline__ void run_irr_direct(const DeviceIrrUnit& u, const Dev
 }
 
 // acc += a * b (complex) as two fused multiply-add chains
-__device__ __forceinline__ void cmac(R& accr, R& acci, R ar, R ai, R br, R bi) {
-  accr = fma(ar, br, accr);
-  accr = fma(-ai, bi, accr);
-  acci = fma(ar, bi, acci);
-  acci = fma(ai, br, acci);
+template <class V>
+__device__ __forceinline__ void cmac(V& accr, V& acci, V ar, V ai, V br, V bi) {
+  accr = vfma(ar, br, accr);
+  accr = vfma(-ai, bi, accr);
+  acci = vfma(ar, bi, acci);
+  acci = vfma(ai, br, acci);
 }
 
 // Element tuples of one irreps (order Q <= 4, TT elements) over a chunk of
@@ -743,19 +841,20 @@ __device__ __forceinline__ void cmac(R& accr, R& acci, R ar, R ai, R br, R bi) {
 // order-parameter loads per term; the adjoint partials of x and y are summed
 // over z in registers and flushed with one shared-memory atomic per (slot,
 // element).
-template <int Q, int TT, int Lh, class EA>
+template <class V, int Q, int TT, int Lh, class EA, class GT>
 __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                         const DeviceTerm* __restrict__ terms,
-                                        const R* __restrict__ wlin, const R* hnl,
-                                        const Rc* sa, R* sg, int gim, GFix& gf, int n,
-                                        int half, bool act, EA& eacc) {
+                                        const V* __restrict__ wlin, const V* hnl,
+                                        const typename Cx<V>::type* sa, GT* sg, int gim,
+                                        GFixT<V>& gf, int n, int half, bool act, EA& eacc) {
+  using Vc = typename Cx<V>::type;
   constexpr int NZ = (Q >= 3) ? TT : 1;      // elements of slot z
   constexpr int NX = TT;                     // elements of slot x (slot 0 for Q = 1)
   constexpr int NY = (Q == 1) ? 1 : TT;      // elements of slot y
   constexpr int PZ = Q - 3;                  // slot indices (PZ, PY unused when absent)
   constexpr int PX = (Q == 1) ? 0 : Q - 2;
   constexpr int PY = Q - 1;
-  R H[NZ][NX][NY];
+  V H[NZ][NX][NY];
 #pragma unroll
   for (int z = 0; z < NZ; ++z)
 #pragma unroll
@@ -769,52 +868,52 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
   const int s0 = (int)u.s0;
   constexpr int es = Lh * kNPad;   // element stride in the a / G arrays
   constexpr int kIm = TT * es, kLo = 2 * kIm;   // imaginary / low-part offsets (T == TT)
-  R eu = R(0);
+  V eu = V(0);
   // the two half-warps take alternate terms; the adjoints of slot z (and of
   // the fixed slot 0 of order 4) are kept in registers while a half-warp's
   // consecutive terms address the same order parameter (runs of the table's
   // outer m loops) and flushed when its next term moves on
   const int ke = u.term0 + u.nterm, kb = u.term0 + half;
-  R azr[NZ], azi[NZ], a0r = R(0), a0i = R(0);
+  V azr[NZ], azi[NZ], a0r = V(0), a0i = V(0);
 #pragma unroll
-  for (int z = 0; z < NZ; ++z) { azr[z] = R(0); azi[z] = R(0); }
+  for (int z = 0; z < NZ; ++z) { azr[z] = V(0); azi[z] = V(0); }
   int4 nxt = kb < ke ? __ldg(reinterpret_cast<const int4*>(terms + kb)) : make_int4(0, 0, 0, 0);
   for (int k = kb; k < ke; k += 2) {
     const int4 raw = nxt;
     if (k + 2 < ke) nxt = __ldg(reinterpret_cast<const int4*>(terms + k + 2));
     const bool last = k + 2 >= ke;
-    const R c = term_coeff(raw);
+    const V c = term_coeff<V>(raw);
     const unsigned lw = (unsigned)raw.z, code = ((unsigned)raw.w) >> 16;
     const bool self = (code >> 12) & 1u;
-    const R ce = self ? c : R(2) * c;
+    const V ce = self ? c : V(2) * c;
     int lo[Q];
 #pragma unroll
     for (int p = 0; p < Q; ++p) lo[p] = (int)((lw >> (8 * p)) & 255u) * kNPad + n;
     const auto conj_of = [&](int p) { return ((code >> (2 * p)) & 3u) == (unsigned)kSlotConj; };
-    R Ar = R(1), Ai = R(0);   // fixed slot 0 of order 4
+    V Ar = V(1), Ai = V(0);   // fixed slot 0 of order 4
     if (Q == 4) {
-      const Rc v = sa[s0 * es + lo[0]];
+      const Vc v = sa[s0 * es + lo[0]];
       Ar = v.x;
       Ai = conj_of(0) ? -v.y : v.y;
     }
-    R zr[NZ], zi[NZ], br[NX], bi[NX], cr[NY], ci[NY];
+    V zr[NZ], zi[NZ], br[NX], bi[NX], cr[NY], ci[NY];
     if (Q >= 3) {
       const bool cj = conj_of(PZ);
 #pragma unroll
       for (int z = 0; z < NZ; ++z) {
-        const Rc v = sa[z * es + lo[PZ]];
+        const Vc v = sa[z * es + lo[PZ]];
         zr[z] = v.x;
         zi[z] = cj ? -v.y : v.y;
       }
     } else {
-      zr[0] = R(1);
-      zi[0] = R(0);
+      zr[0] = V(1);
+      zi[0] = V(0);
     }
     {
       const bool cj = conj_of(PX);
 #pragma unroll
       for (int x = 0; x < NX; ++x) {
-        const Rc v = sa[x * es + lo[PX]];
+        const Vc v = sa[x * es + lo[PX]];
         br[x] = v.x;
         bi[x] = cj ? -v.y : v.y;
       }
@@ -823,38 +922,38 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       const bool cj = conj_of(PY);
 #pragma unroll
       for (int y = 0; y < NY; ++y) {
-        const Rc v = sa[y * es + lo[PY]];
+        const Vc v = sa[y * es + lo[PY]];
         cr[y] = v.x;
         ci[y] = cj ? -v.y : v.y;
       }
     }
     // adjoint partials summed over z: x and y (before the prefix A), and S
-    R gxr[NX], gxi[NX], gyr[NY], gyi[NY], gzr[NZ], gzi[NZ];
-    R Sr = R(0), Si = R(0);
+    V gxr[NX], gxi[NX], gyr[NY], gyi[NY], gzr[NZ], gzi[NZ];
+    V Sr = V(0), Si = V(0);
 #pragma unroll
-    for (int x = 0; x < NX; ++x) { gxr[x] = R(0); gxi[x] = R(0); }
+    for (int x = 0; x < NX; ++x) { gxr[x] = V(0); gxi[x] = V(0); }
 #pragma unroll
-    for (int y = 0; y < NY; ++y) { gyr[y] = R(0); gyi[y] = R(0); }
+    for (int y = 0; y < NY; ++y) { gyr[y] = V(0); gyi[y] = V(0); }
 #pragma unroll
     for (int z = 0; z < NZ; ++z) {
-      R mr[NX], mi[NX];
+      V mr[NX], mi[NX];
 #pragma unroll
       for (int x = 0; x < NX; ++x) {
         if (Q == 1) {
           mr[x] = H[0][x][0];
-          mi[x] = R(0);
+          mi[x] = V(0);
         } else {
-          R tr = R(0), ti = R(0);
+          V tr = V(0), ti = V(0);
 #pragma unroll
           for (int y = 0; y < NY; ++y) {
-            tr = fma(H[z][x][y], cr[y], tr);
-            ti = fma(H[z][x][y], ci[y], ti);
+            tr = vfma(H[z][x][y], cr[y], tr);
+            ti = vfma(H[z][x][y], ci[y], ti);
           }
           mr[x] = tr;
           mi[x] = ti;
         }
       }
-      R szr = R(0), szi = R(0);
+      V szr = V(0), szi = V(0);
 #pragma unroll
       for (int x = 0; x < NX; ++x) {
         cmac(szr, szi, br[x], bi[x], mr[x], mi[x]);
@@ -869,11 +968,11 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       if (Q > 1) {
 #pragma unroll
         for (int y = 0; y < NY; ++y) {
-          R tr = R(0), ti = R(0);
+          V tr = V(0), ti = V(0);
 #pragma unroll
           for (int x = 0; x < NX; ++x) {
-            tr = fma(H[z][x][y], br[x], tr);
-            ti = fma(H[z][x][y], bi[x], ti);
+            tr = vfma(H[z][x][y], br[x], tr);
+            ti = vfma(H[z][x][y], bi[x], ti);
           }
           cmac(gyr[y], gyi[y], zr[z], zi[z], tr, ti);
         }
@@ -884,12 +983,12 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       // adjoint of slot p: A * partial, scaled by (kr, ki) from its storage
       // code; unconditional (lanes n >= F and unused imaginary parts add
       // exact zeros), so the flush has no divergent branches
-      const R cs = c * gf.scale;
-      const auto flush = [&](int p, int e, R vr, R vi) {
+      const V cs = gscale(c, gf);
+      const auto flush = [&](int p, int e, V vr, V vi) {
         const unsigned cd = (code >> (2 * p)) & 3u;
-        const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * cs : cs;
-        const R ki = (cd == 0u) ? cs : (cd == 1u ? -cs : R(0));
-        R* gp = sg + e * es + lo[p];
+        const V kr = (cd == (unsigned)kSlotMZero) ? V(2) * cs : cs;
+        const V ki = (cd == 0u) ? cs : (cd == 1u ? -cs : V(0));
+        GT* gp = sg + e * es + lo[p];
         gput(gp, kr * (Ar * vr - Ai * vi), gf, kLo);
         gput(gp + kIm, ki * (Ar * vi + Ai * vr), gf, kLo);
       };
@@ -902,9 +1001,9 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
     }
     if (Q >= 3) {   // slot z: A S_z, accumulated over the run
       const unsigned cd = (code >> (2 * PZ)) & 3u;
-      const R cs = c * gf.scale;
-      const R kr = (cd == (unsigned)kSlotMZero) ? R(2) * cs : cs;
-      const R ki = (cd == 0u) ? cs : (cd == 1u ? -cs : R(0));
+      const V cs = gscale(c, gf);
+      const V kr = (cd == (unsigned)kSlotMZero) ? V(2) * cs : cs;
+      const V ki = (cd == 0u) ? cs : (cd == 1u ? -cs : V(0));
 #pragma unroll
       for (int z = 0; z < NZ; ++z) {
         azr[z] += kr * (Ar * gzr[z] - Ai * gzi[z]);
@@ -916,26 +1015,26 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
       if (__any_sync(__activemask(), need)) {
 #pragma unroll
         for (int z = 0; z < NZ; ++z) {
-          R* gp = sg + z * es + lo[PZ];
+          GT* gp = sg + z * es + lo[PZ];
           gput(gp, azr[z], gf, kLo);
           gput(gp + kIm, azi[z], gf, kLo);
         }
 #pragma unroll
-        for (int z = 0; z < NZ; ++z) { azr[z] = R(0); azi[z] = R(0); }
+        for (int z = 0; z < NZ; ++z) { azr[z] = V(0); azi[z] = V(0); }
       }
     }
     if (Q == 4) {   // slot 0: S, without the prefix A (it is slot 0's own factor)
       const unsigned cd = code & 3u;
-      const R cs = c * gf.scale;
-      a0r += ((cd == (unsigned)kSlotMZero) ? R(2) * cs : cs) * Sr;
-      a0i += ((cd == 0u) ? cs : (cd == 1u ? -cs : R(0))) * Si;
+      const V cs = gscale(c, gf);
+      a0r += ((cd == (unsigned)kSlotMZero) ? V(2) * cs : cs) * Sr;
+      a0i += ((cd == 0u) ? cs : (cd == 1u ? -cs : V(0))) * Si;
       const bool need0 = last || (((unsigned)nxt.z ^ lw) & 255u) != 0u;
       if (__any_sync(__activemask(), need0)) {
-        R* gp = sg + s0 * es + lo[0];
+        GT* gp = sg + s0 * es + lo[0];
         gput(gp, a0r, gf, kLo);
         gput(gp + kIm, a0i, gf, kLo);
-        a0r = R(0);
-        a0i = R(0);
+        a0r = V(0);
+        a0i = V(0);
       }
     }
   }
@@ -944,38 +1043,290 @@ __device__ __forceinline__ void run_irr(const DeviceIrrUnit& u, const DeviceTupl
   eadd(eacc, eu);
 }
 
-template <int TT, int Lh, class EA>
+// pick of entry z (a runtime index below N) of a register array by selects
+// (no local-memory indexing)
+template <int N>
+__device__ __forceinline__ DF pick(int z, const DF (&v)[N]) {
+  DF r = v[0];
+#pragma unroll
+  for (int k = 1; k < N; ++k) r = (z == k) ? v[k] : r;
+  return r;
+}
+
+// Double-float form of run_irr (same algebra, same flushes).  The element
+// loop over slot z is kept rolled (the operands of the current z are picked
+// from registers by selects): fully unrolled, the double-float body of one
+// term outgrows the instruction cache and the warps wait on instruction
+// fetch.  Sums go through DFA accumulators (one FP32 add of dependency per
+// accumulation), products of accumulated values are renormalised once.
+template <int Q, int TT, int Lh, class EA>
+__device__ __forceinline__ void run_irr_df(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
+                                           const DeviceTerm* __restrict__ terms,
+                                           const DF* __restrict__ wlin, const DF* hnl,
+                                           const DFc* sa, int* sg, int gim, GFixT<DF>& gf, int n,
+                                           int half, bool act, EA& eacc) {
+  constexpr int NZ = (Q >= 3) ? TT : 1;      // elements of slot z
+  constexpr int NX = TT;                     // elements of slot x (slot 0 for Q = 1)
+  constexpr int NY = (Q == 1) ? 1 : TT;      // elements of slot y
+  constexpr int PZ = (Q >= 3) ? Q - 3 : 0;   // slot indices
+  constexpr int PX = (Q == 1) ? 0 : Q - 2;
+  constexpr int PY = Q - 1;
+  DF H[NZ][NX * NY];
+#pragma unroll
+  for (int z = 0; z < NZ; ++z)
+#pragma unroll
+    for (int j = 0; j < NX * NY; ++j) {
+      const int2 e = __ldg(reinterpret_cast<const int2*>(tups + u.tup + z * NX * NY + j));
+      H[z][j] = tuple_weight(e, wlin, hnl, n, act);
+    }
+  const int s0 = (int)u.s0;
+  constexpr int es = Lh * kNPad;                // element stride in the a / G arrays
+  constexpr int kIm = TT * es, kLo = 2 * kIm;   // imaginary / next-word offsets (T == TT)
+  DF eu = DF(0.0f);
+  const int ke = u.term0 + u.nterm, kb = u.term0 + half;
+  DF azr[NZ], azi[NZ], a0r = DF(0.0f), a0i = DF(0.0f);
+#pragma unroll
+  for (int z = 0; z < NZ; ++z) { azr[z] = DF(0.0f); azi[z] = DF(0.0f); }
+  int4 nxt = kb < ke ? __ldg(reinterpret_cast<const int4*>(terms + kb)) : make_int4(0, 0, 0, 0);
+  for (int k = kb; k < ke; k += 2) {
+    const int4 raw = nxt;
+    if (k + 2 < ke) nxt = __ldg(reinterpret_cast<const int4*>(terms + k + 2));
+    const bool last = k + 2 >= ke;
+    const DF c = term_coeff<DF>(raw);
+    const unsigned lw = (unsigned)raw.z, code = ((unsigned)raw.w) >> 16;
+    const bool self = (code >> 12) & 1u;
+    int lo[Q];
+#pragma unroll
+    for (int p = 0; p < Q; ++p) lo[p] = (int)((lw >> (8 * p)) & 255u) * kNPad + n;
+    const auto conj_of = [&](int p) { return ((code >> (2 * p)) & 3u) == (unsigned)kSlotConj; };
+    DF Ar = DF(1.0f), Ai = DF(0.0f);   // fixed slot 0 of order 4
+    if (Q == 4) {
+      const DFc v = sa[s0 * es + lo[0]];
+      Ar = v.x;
+      Ai = conj_of(0) ? -v.y : v.y;
+    }
+    DF zr[NZ], zi[NZ], br[NX], bi[NX], cr[NY], ci[NY];
+    if (Q >= 3) {
+      const bool cj = conj_of(PZ);
+#pragma unroll
+      for (int z = 0; z < NZ; ++z) {
+        const DFc v = sa[z * es + lo[PZ]];
+        zr[z] = v.x;
+        zi[z] = cj ? -v.y : v.y;
+      }
+    } else {
+      zr[0] = DF(1.0f);
+      zi[0] = DF(0.0f);
+    }
+    {
+      const bool cj = conj_of(PX);
+#pragma unroll
+      for (int x = 0; x < NX; ++x) {
+        const DFc v = sa[x * es + lo[PX]];
+        br[x] = v.x;
+        bi[x] = cj ? -v.y : v.y;
+      }
+    }
+    if (Q > 1) {
+      const bool cj = conj_of(PY);
+#pragma unroll
+      for (int y = 0; y < NY; ++y) {
+        const DFc v = sa[y * es + lo[PY]];
+        cr[y] = v.x;
+        ci[y] = cj ? -v.y : v.y;
+      }
+    } else {
+      cr[0] = DF(1.0f);
+      ci[0] = DF(0.0f);
+    }
+    DFA Sr, Si, gxr[NX], gxi[NX], gyr[NY], gyi[NY];
+    DF gzr[NZ], gzi[NZ];
+#pragma unroll
+    for (int z = 0; z < NZ; ++z) { gzr[z] = DF(0.0f); gzi[z] = DF(0.0f); }
+#pragma unroll 1
+    for (int z = 0; z < NZ; ++z) {
+      DF Hc[NX * NY];
+#pragma unroll
+      for (int j = 0; j < NX * NY; ++j) {
+        Hc[j] = H[0][j];
+#pragma unroll
+        for (int q = 1; q < NZ; ++q) Hc[j] = (z == q) ? H[q][j] : Hc[j];
+      }
+      const DF ar = pick(z, zr), ai = pick(z, zi);
+      // m[x] = sum_y H c[y]
+      DF mr[NX], mi[NX];
+#pragma unroll
+      for (int x = 0; x < NX; ++x) {
+        if (Q == 1) {
+          mr[x] = Hc[x];
+          mi[x] = DF(0.0f);
+        } else {
+          DFA tr, ti;
+#pragma unroll
+          for (int y = 0; y < NY; ++y) {
+            acc_fma(tr, Hc[x * NY + y], cr[y]);
+            acc_fma(ti, Hc[x * NY + y], ci[y]);
+          }
+          mr[x] = acc_val(tr);
+          mi[x] = acc_val(ti);
+        }
+      }
+      // S_z = sum_x b[x] m[x]
+      DFA szr, szi;
+#pragma unroll
+      for (int x = 0; x < NX; ++x) cacc(szr, szi, br[x], bi[x], mr[x], mi[x]);
+      const DF sr = acc_val(szr), si = acc_val(szi);
+      if (Q >= 3) {
+#pragma unroll
+        for (int q = 0; q < NZ; ++q) {
+          gzr[q] = (z == q) ? sr : gzr[q];
+          gzi[q] = (z == q) ? si : gzi[q];
+        }
+        cacc(Sr, Si, ar, ai, sr, si);
+#pragma unroll
+        for (int x = 0; x < NX; ++x) cacc(gxr[x], gxi[x], ar, ai, mr[x], mi[x]);
+      } else {
+        acc_add(Sr, sr);
+        acc_add(Si, si);
+#pragma unroll
+        for (int x = 0; x < NX; ++x) { acc_add(gxr[x], mr[x]); acc_add(gxi[x], mi[x]); }
+      }
+      if (Q > 1) {
+#pragma unroll
+        for (int y = 0; y < NY; ++y) {
+          DFA tr, ti;
+#pragma unroll
+          for (int x = 0; x < NX; ++x) {
+            acc_fma(tr, Hc[x * NY + y], br[x]);
+            acc_fma(ti, Hc[x * NY + y], bi[x]);
+          }
+          if (Q >= 3) {
+            cacc(gyr[y], gyi[y], ar, ai, acc_val(tr), acc_val(ti));
+          } else {
+            gyr[y] = tr;
+            gyi[y] = ti;
+          }
+        }
+      }
+    }
+    const DF Sv = acc_val(Sr), Siv = acc_val(Si);
+    const DF ce = self ? c : DF(2.0f) * c;
+    eu += ce * (Q == 4 ? Ar * Sv - Ai * Siv : Sv);
+    {
+      // adjoint of slot p: A * partial, scaled by (kr, ki) from its storage
+      // code; unconditional (lanes n >= F and unused imaginary parts add
+      // exact zeros)
+      const DF cs = gscale(c, gf);
+      const auto flush = [&](int p, int e, DF vr, DF vi) {
+        const unsigned cd = (code >> (2 * p)) & 3u;
+        const DF kr = (cd == (unsigned)kSlotMZero) ? DF(2.0f) * cs : cs;
+        const DF ki = (cd == 0u) ? cs : (cd == 1u ? -cs : DF(0.0f));
+        int* gp = sg + e * es + lo[p];
+        if (Q == 4) {
+          gput(gp, kr * (Ar * vr - Ai * vi), gf, kLo);
+          gput(gp + kIm, ki * (Ar * vi + Ai * vr), gf, kLo);
+        } else {
+          gput(gp, kr * vr, gf, kLo);
+          gput(gp + kIm, ki * vi, gf, kLo);
+        }
+      };
+#pragma unroll
+      for (int x = 0; x < NX; ++x) flush(PX, x, acc_val(gxr[x]), acc_val(gxi[x]));
+      if (Q > 1) {
+#pragma unroll
+        for (int y = 0; y < NY; ++y) flush(PY, y, acc_val(gyr[y]), acc_val(gyi[y]));
+      }
+    }
+    if (Q >= 3) {   // slot z: A S_z, accumulated over the run
+      const unsigned cd = (code >> (2 * PZ)) & 3u;
+      const DF cs = gscale(c, gf);
+      const DF kr = (cd == (unsigned)kSlotMZero) ? DF(2.0f) * cs : cs;
+      const DF ki = (cd == 0u) ? cs : (cd == 1u ? -cs : DF(0.0f));
+#pragma unroll
+      for (int z = 0; z < NZ; ++z) {
+        if (Q == 4) {
+          azr[z] += kr * (Ar * gzr[z] - Ai * gzi[z]);
+          azi[z] += ki * (Ar * gzi[z] + Ai * gzr[z]);
+        } else {
+          azr[z] += kr * gzr[z];
+          azi[z] += ki * gzi[z];
+        }
+      }
+      const bool need = last || ((((unsigned)nxt.z ^ lw) >> (8 * PZ)) & 255u) != 0u;
+      if (__any_sync(__activemask(), need)) {
+#pragma unroll
+        for (int z = 0; z < NZ; ++z) {
+          int* gp = sg + z * es + lo[PZ];
+          gput(gp, azr[z], gf, kLo);
+          gput(gp + kIm, azi[z], gf, kLo);
+        }
+#pragma unroll
+        for (int z = 0; z < NZ; ++z) { azr[z] = DF(0.0f); azi[z] = DF(0.0f); }
+      }
+    }
+    if (Q == 4) {   // slot 0: S, without the prefix A (it is slot 0's own factor)
+      const unsigned cd = code & 3u;
+      const DF cs = gscale(c, gf);
+      a0r += ((cd == (unsigned)kSlotMZero) ? DF(2.0f) * cs : cs) * Sv;
+      a0i += ((cd == 0u) ? cs : (cd == 1u ? -cs : DF(0.0f))) * Siv;
+      const bool need0 = last || (((unsigned)nxt.z ^ lw) & 255u) != 0u;
+      if (__any_sync(__activemask(), need0)) {
+        int* gp = sg + s0 * es + lo[0];
+        gput(gp, a0r, gf, kLo);
+        gput(gp + kIm, a0i, gf, kLo);
+        a0r = DF(0.0f);
+        a0i = DF(0.0f);
+      }
+    }
+  }
+  // this half-warp's terms into the thread's energy sum (zero on lanes n >= F)
+  eadd(eacc, eu);
+}
+
+template <class V, int TT, int Lh, class EA, class GT>
 __device__ __forceinline__ void dispatch_irr(const DeviceIrrUnit& u, const DeviceTuple* tups,
-                                             const DeviceTerm* terms, const R* wlin,
-                                             const R* hnl, const Rc* sa, R* sg, int gim,
-                                             GFix& gf, int n, int half, bool act, EA& eacc) {
+                                             const DeviceTerm* terms, const V* wlin,
+                                             const V* hnl, const typename Cx<V>::type* sa,
+                                             GT* sg, int gim, GFixT<V>& gf, int n, int half,
+                                             bool act, EA& eacc) {
+  if constexpr (std::is_same_v<V, DF>) {
+    switch (u.q) {
+      case 1: run_irr_df<1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+      case 2: run_irr_df<2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+      case 3: run_irr_df<3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+      default: run_irr_df<4, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+    }
+    return;
+  } else {
   if (TT <= 2 && u.q <= 3) {
     switch (u.q) {
-      case 1: run_irr_direct<1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
-      case 2: run_irr_direct<2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
-      default: run_irr_direct<3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+      case 1: run_irr_direct<V, 1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+      case 2: run_irr_direct<V, 2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+      default: run_irr_direct<V, 3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
     }
     return;
   }
   switch (u.q) {
-    case 1: run_irr<1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
-    case 2: run_irr<2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
-    case 3: run_irr<3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
-    default: run_irr<4, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+    case 1: run_irr<V, 1, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+    case 2: run_irr<V, 2, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+    case 3: run_irr<V, 3, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+    default: run_irr<V, 4, TT, Lh>(u, tups, terms, wlin, hnl, sa, sg, gim, gf, n, half, act, eacc); break;
+  }
   }
 }
 
-template <bool WITH_G, int Lh>
+template <class V, bool WITH_G, int Lh, class GT>
 __device__ __forceinline__ void dispatch_unit(const DeviceUnit& u, const DeviceTerm* terms,
-                                              const Rc* sa, R* sg, int gim, GFix& gf, int n,
-                                              int half, bool act, R H, R& dsum) {
+                                              const typename Cx<V>::type* sa, GT* sg, int gim,
+                                              GFixT<V>& gf, int n, int half, bool act, V H,
+                                              V& dsum) {
   switch (u.q) {
-    case 1: run_unit<1, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
-    case 2: run_unit<2, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
-    case 3: run_unit<3, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
-    case 4: run_unit<4, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
-    case 5: run_unit<5, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
-    default: run_unit<6, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    case 1: run_unit<V, 1, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    case 2: run_unit<V, 2, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    case 3: run_unit<V, 3, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    case 4: run_unit<V, 4, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    case 5: run_unit<V, 5, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
+    default: run_unit<V, 6, WITH_G, Lh>(u, terms, sa, sg, gim, gf, n, half, act, H, dsum); break;
   }
 }
 
@@ -1150,8 +1501,9 @@ __host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int
                                                   int lh64) {
   SmemLayout s;
   const size_t an = (size_t)T * Lh * kNPad * sizeof(Rc);
-  // adjoint: FP64 re/im, or the mixed path's int32 high + low parts of re/im
-  const size_t gn = (size_t)T * Lh * kNPad * 16;
+  // adjoint: FP64 re/im, the mixed path's int32 high + low parts of re/im,
+  // or the double-float path's four int32 words of re/im
+  const size_t gn = (size_t)T * Lh * kNPad * (4 * kGWords);
   const size_t stage = (size_t)Lh * kChunk * sizeof(double2) + (size_t)kChunk * kNPad * sizeof(double);
   s.a = 0;
   s.g = align16(an);
@@ -1445,9 +1797,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         if (sizeof(R) == 4 && A.lh64 > 0) {
           dd = nl_forward64(un, A.terms64, a64, A.lh64, n, half);
         } else {
+          // (the double-float path's FP64 table is terms64)
           R dsum = R(0);
-          GFix gnone{R(1), R(0)};
-          dispatch_unit<false, LS>(un, A.terms, sa, sg, gim, gnone, n, half, act, R(0), dsum);
+          GFixT<R> gnone{R(1), R(0)};
+          dispatch_unit<R, false, LS>(un, kDF ? A.terms64 : A.terms, sa, sg, gim, gnone, n, half,
+                                      act, R(0), dsum);
           dd = (double)dsum;
         }
         dd += __shfl_xor_sync(0xffffffffu, dd, 16);
@@ -1510,13 +1864,28 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     // ---------------------------------------------------------------- P4
     // the batched units add hnl to the FP32 weights of every tuple: the mixed
     // path reads an FP32 copy (in the space of dnl, which is no longer read)
-    const R* hnlR = reinterpret_cast<const R*>(hnl);
+    const P* hnlR = reinterpret_cast<const P*>(hnl);
     if constexpr (sizeof(R) == 4) {
       __syncthreads();   // every thread's reads of dnl are done
       float* hf = reinterpret_cast<float*>(dnl);
       for (int e = tid; e < nNL * kNPad; e += kBlock) hf[e] = (float)hnl[e];
-      hnlR = reinterpret_cast<const R*>(hf);   // visible after the barrier below
+      hnlR = reinterpret_cast<const P*>(hf);   // visible after the barrier below
     }
+    if constexpr (kDF) {
+      // double-float path: hnl and the order parameters split into (high,
+      // low) FP32 pairs, the latter in place (16 bytes per complex entry
+      // either way; each thread converts the entries it reads)
+      __syncthreads();   // every thread's reads of dnl and of a (P3) are done
+      DF* hd = reinterpret_cast<DF*>(dnl);
+      for (int e = tid; e < nNL * kNPad; e += kBlock) hd[e] = df_from_double(hnl[e]);
+      hnlR = reinterpret_cast<const P*>(hd);
+      for (int e = tid; e < T * LS * kNPad; e += kBlock) {
+        const double2 v = reinterpret_cast<const double2*>(sa)[e];
+        reinterpret_cast<DFc*>(sa)[e] = DFc{df_from_double(v.x), df_from_double(v.y)};
+      }
+    }
+    const Pc* sp = reinterpret_cast<const Pc*>(sa);
+    PG* sgp = reinterpret_cast<PG*>(sg);
     MLIPG_STAMP(2)
     // ---------------------------------------------------------------- P5
     // (mixed path: redone once at the measured scale if a flush left the
@@ -1524,7 +1893,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     const double eacc0 = eacc;
     int gexp = 0;
     for (int attempt = 0;; ++attempt) {
-    for (int e = tid; e < (sizeof(R) == 4 ? 4 : 2) * gim; e += kBlock) sg[e] = R(0);
+    for (int e = tid; e < kGWords * gim; e += kBlock) reinterpret_cast<int*>(sg)[e] = 0;
     gexp = misc[16 + ti];
     if (tid == 0) {
       misc[12] = 0;
@@ -1533,7 +1902,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       reinterpret_cast<unsigned long long*>(misc + 24)[1] = 0ull;
     }
     __syncthreads();   // G zeroed; everyone has read this attempt's scale
-    GFix gf{sizeof(R) == 4 ? (R)ldexpf(1.0f, gexp) : R(1), R(0)};
+    GFixT<P> gf;
+    if constexpr (kFixG) gf = GFixT<P>{ldexpf(1.0f, gexp), 0.0f};
+    else gf = GFixT<P>{P(1), P(0)};
     ESumF esum;   // mixed path: this thread's energy of the statically dealt units
     {
       const int u0 = __ldg(A.unit_off + ti), nU = __ldg(A.unit_off + ti + 1) - u0;
@@ -1541,14 +1912,14 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       // warp orders 0 and 1 deal the units to the warps statically (each
       // thread's energy sum has a fixed order, so energies are reproducible);
       // order 2 hands them out from a shared counter (below)
-      const R* wl = wlin_table(A);
+      const P* wl = wlin_table(A);
       const auto run_iu = [&](const DeviceIrrUnit& iu, auto& e) {
         if (T == 3)
-          dispatch_irr<3, LS>(iu, A.tuples, A.terms, wl, hnlR, sa, sg, gim, gf, n, half, act, e);
+          dispatch_irr<P, 3, LS>(iu, A.tuples, A.terms, wl, hnlR, sp, sgp, gim, gf, n, half, act, e);
         else if (T == 2)
-          dispatch_irr<2, LS>(iu, A.tuples, A.terms, wl, hnlR, sa, sg, gim, gf, n, half, act, e);
+          dispatch_irr<P, 2, LS>(iu, A.tuples, A.terms, wl, hnlR, sp, sgp, gim, gf, n, half, act, e);
         else
-          dispatch_irr<1, LS>(iu, A.tuples, A.terms, wl, hnlR, sa, sg, gim, gf, n, half, act, e);
+          dispatch_irr<P, 1, LS>(iu, A.tuples, A.terms, wl, hnlR, sp, sgp, gim, gf, n, half, act, e);
       };
       if (A.unit_dyn) {
         // warps take units from a shared counter (no end-of-phase imbalance);
@@ -1582,7 +1953,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           __syncwarp();   // every lane has read the slot before it is refilled
           const int un = take();
           fetch(un);
-          std::conditional_t<sizeof(R) == 4, ESumF, double> eu{};
+          EU eu{};
           run_iu(cur, eu);
           const double e = warp_energy(eu);
           // units of the polynomial's input features: energy taken in P3
@@ -1597,7 +1968,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         for (int u = warp; u < nI; u += kBlock / 32) {
           const DeviceIrrUnit iu = A.iunits[i0 + u];
           if (iu.nterm == 0) continue;   // padding of a balanced schedule
-          std::conditional_t<sizeof(R) == 4, ESumF, double> eu{};
+          EU eu{};
           run_iu(iu, eu);
           // units of the polynomial's input features: energy taken in P3
           if (!iu.nl) merge_unit_energy(esum, eacc, eu);
@@ -1612,13 +1983,13 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           hv = __ldg(A.w_lin + (size_t)un.itc * kNPad + n);
           if (un.nl_slot >= 0) hv += hnl[un.nl_slot * kNPad + n];
         }
-        R dsum = R(0);
-        dispatch_unit<true, LS>(un, A.terms, sa, sg, gim, gf, n, half, act, (R)hv, dsum);
-        dsum += __shfl_xor_sync(0xffffffffu, dsum, 16);
-        if (half == 0 && act && un.nl_slot < 0) eacc += hv * (double)dsum;
+        P dsum = P(0);
+        dispatch_unit<P, true, LS>(un, A.terms, sp, sgp, gim, gf, n, half, act, to_p(hv), dsum);
+        const double ds = half_pair_sum(dsum);
+        if (half == 0 && act && un.nl_slot < 0) eacc += hv * ds;
       }
     }
-    if (sizeof(R) != 4) {
+    if constexpr (!kFixG) {
       __syncthreads();
       if (A.unit_dyn && tid == 0)
         eacc += unit_energy(misc);
@@ -1640,7 +2011,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       // next scale: the largest flush at half the bound
       int lv = ilogbf(vm);
       if (vm > ldexpf(1.0f, lv)) ++lv;
-      misc[16 + ti] = max(-120, min(120, gexp + ilogbf(A.g_bound) - 1 - lv));
+      // (capped so that a coefficient times the scale stays finite)
+      misc[16 + ti] = max(-120, min(100, gexp + ilogbf(A.g_bound) - 1 - lv));
     }
     if ((!out && !coarse) || attempt >= 2) {
       if (out && tid == 0) atomicOr(A.status, kStatusAdjointRange);
@@ -1659,6 +2031,21 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       const int* gi = reinterpret_cast<const int*>(sg);
       for (int e = tid; e < 2 * gim; e += kBlock)
         sg[e] = (R)(fmaf((float)gi[e], 65536.0f, (float)gi[e + 2 * gim]) * inv);
+      __syncthreads();
+    }
+    // double-float path: the four words -> FP64 adjoint in the space of a
+    // (not read again for this centre)
+    R* gP6 = sg;
+    if constexpr (kDF) {
+      __syncthreads();
+      const double inv = ldexp(1.0, -gexp);
+      const int* gw = reinterpret_cast<const int*>(sg);
+      double* gd = reinterpret_cast<double*>(sa);
+      for (int e = tid; e < 2 * gim; e += kBlock) {
+        const double lo2 = (double)gw[e + 4 * gim] * 65536.0 + (double)gw[e + 6 * gim];  // exact
+        gd[e] = fma((double)gw[e], 0x1p48, fma((double)gw[e + 2 * gim], 0x1p32, lo2)) * inv;
+      }
+      gP6 = reinterpret_cast<R*>(gd);
       __syncthreads();
     }
     MLIPG_STAMP(4)
@@ -1683,7 +2070,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         R f[4], fd[4];
         radial4(A.radial, F, n0, (R)r, rc, f, fd);
         const double ir = 1.0 / r;
-        ForceVis v{sg + (size_t)tj * LS * kNPad + n0, gim, f, fd, (R)(dx * ir), (R)(dy * ir),
+        ForceVis v{gP6 + (size_t)tj * LS * kNPad + n0, gim, f, fd, (R)(dx * ir), (R)(dy * ir),
                    (R)(dz * ir), R(0), R(0), R(0)};
         sh_visit<LCAP, true>((R)dx, (R)dy, (R)dz, (R)r, L, v);
         double fx = v.fx, fy = v.fy, fz = v.fz;

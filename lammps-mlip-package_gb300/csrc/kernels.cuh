@@ -47,6 +47,7 @@ struct KernelArgs {
   const DeviceAdj* adj;   // (term weight, other factors) per gather entry
   const double* w_lin;    // [n_itc][16]
   const float* w_lin_f;   // [n_itc][16], FP32 copy for the mixed path
+  const float2* w_lin_df; // [n_itc][16], (high, low) FP32 pairs for the double-float path
   const double* radial;   // [F][2] (beta, mu)
   // radial-only descriptor (pair potentials, pair.cu)
   const DevicePairTerm* pair_terms;
@@ -62,7 +63,7 @@ struct KernelArgs {
   double rec_q;
   int T, F, L, Lh, nb_cap, nl_cap;
   double rc;
-  float g_bound;          // mixed path: largest fixed-point adjoint flush (power of two)
+  float g_bound;          // fixed-point paths: largest adjoint flush (power of two)
   int unit_dyn;           // 1: warps take batched units from a shared counter
   int sum64;              // mixed path: order-parameter sums in plain FP64 FMAs
   int lh64;               // mixed path: rows of FP64 order parameters (0 = none)
@@ -75,9 +76,13 @@ struct KernelArgs {
   unsigned long long* phase_clocks;  // optional [8]: SM cycles spent per phase (P1..P6)
 };
 
-size_t fused_smem_bytes(bool fp64, int T, int L, int nb_cap, int nl_cap, int lh64);
-int fused_max_blocks_per_sm(bool fp64, int L, size_t smem);
-cudaError_t launch_fused(bool fp64, int L, const KernelArgs& a, int grid, size_t smem,
+// Instantiations of the fused kernel: FP32 products (the mixed
+// precisions), FP64 throughout, and FP64 with the invariant/adjoint phase in
+// double-float arithmetic.
+enum KernelVariant { kVariantF32 = 0, kVariantF64 = 1, kVariantF64DF = 2 };
+size_t fused_smem_bytes(int variant, int T, int L, int nb_cap, int nl_cap, int lh64);
+int fused_max_blocks_per_sm(int variant, int L, size_t smem);
+cudaError_t launch_fused(int variant, int L, const KernelArgs& a, int grid, size_t smem,
                          cudaStream_t s);
 // Sums the per-CTA partials in a fixed order into out8[0..6] and writes the
 // launch's status bits (as a double) into out8[7].
@@ -101,6 +106,7 @@ namespace mlipg {
   cudaError_t init_constants();                                                        \
   }
 MLIPG_DECL_PREC(f64)
+MLIPG_DECL_PREC(f64df)
 MLIPG_DECL_PREC(f32)
 #undef MLIPG_DECL_PREC
 }  // namespace mlipg

@@ -8,22 +8,34 @@ static_assert(kBlock / 32 == kCtaWarps, "schedules are dealt to the CTA's warps"
 static_assert(sizeof(DeviceUnit) == 32, "DeviceUnit must be 32 bytes");
 static_assert(sizeof(DevicePoly) == 32, "DevicePoly must be 32 bytes");
 
-size_t fused_smem_bytes(bool fp64, int T, int L, int nb_cap, int nl_cap, int lh64) {
-  return fp64 ? f64::smem_bytes(T, L, nb_cap, nl_cap, 0)
-              : f32::smem_bytes(T, L, nb_cap, nl_cap, lh64);
+size_t fused_smem_bytes(int variant, int T, int L, int nb_cap, int nl_cap, int lh64) {
+  switch (variant) {
+    case kVariantF64: return f64::smem_bytes(T, L, nb_cap, nl_cap, 0);
+    case kVariantF64DF: return f64df::smem_bytes(T, L, nb_cap, nl_cap, 0);
+    default: return f32::smem_bytes(T, L, nb_cap, nl_cap, lh64);
+  }
 }
 
-int fused_max_blocks_per_sm(bool fp64, int L, size_t smem) {
-  return fp64 ? f64::max_blocks(L, smem) : f32::max_blocks(L, smem);
+int fused_max_blocks_per_sm(int variant, int L, size_t smem) {
+  switch (variant) {
+    case kVariantF64: return f64::max_blocks(L, smem);
+    case kVariantF64DF: return f64df::max_blocks(L, smem);
+    default: return f32::max_blocks(L, smem);
+  }
 }
 
-cudaError_t launch_fused(bool fp64, int L, const KernelArgs& a, int grid, size_t smem,
+cudaError_t launch_fused(int variant, int L, const KernelArgs& a, int grid, size_t smem,
                          cudaStream_t s) {
-  return fp64 ? f64::launch(L, a, grid, smem, s) : f32::launch(L, a, grid, smem, s);
+  switch (variant) {
+    case kVariantF64: return f64::launch(L, a, grid, smem, s);
+    case kVariantF64DF: return f64df::launch(L, a, grid, smem, s);
+    default: return f32::launch(L, a, grid, smem, s);
+  }
 }
 
 cudaError_t init_device_constants() {
   cudaError_t e = f64::init_constants();
+  if (e == cudaSuccess) e = f64df::init_constants();
   if (e != cudaSuccess) return e;
   return f32::init_constants();
 }

@@ -350,6 +350,19 @@ void set_adjoint_bound(Model& M) {
   double b = 274877906944.0;   // 2^38
   while ((b / 65536.0) * (cmax + 1) >= 2147483648.0 && b > 65536.0) b *= 0.5;
   M.g_bound = cmax < 65535 ? b : 0.0;   // 0: no fixed-point accumulation possible
+  // double-float path: four words, multiples of 2^48 (at most bound / 2^48
+  // each, int32 sum below 2^31), of 2^32, 2^16 and 1 (at most 2^16 + 2 per
+  // flush: fewer than 2^15 - 2 flushes cannot overflow); the split's
+  // magic-number roundings are exact below 2^70
+  double bd = 1180591620717411303424.0;   // 2^70
+  while ((bd / 281474976710656.0) * (cmax + 1) >= 2147483648.0 && bd > 65536.0) bd *= 0.5;
+  M.g_bound_df = cmax < 32765 ? bd : 0.0;
+  // the double-float path has FP32's exponent range: potentials whose
+  // coefficients come near it (|.| > 1e30) run the all-FP64 kernel instead
+  double cmaxabs = 0.0;
+  for (double v : M.pot.coeffs) cmaxabs = std::max(cmaxabs, std::fabs(v));
+  for (const DeviceTerm& t : M.cterms) cmaxabs = std::max(cmaxabs, std::fabs(t.c));
+  if (!(cmaxabs <= 1e30)) M.g_bound_df = 0.0;
 }
 
 bool schedules_for_tiling(Model& M, std::string& err) {

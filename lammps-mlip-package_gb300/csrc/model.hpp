@@ -180,6 +180,7 @@ struct Model {
   // adjoint accumulation (high parts in multiples of 2^16): a power of two with
   // (flushes per entry) x bound / 2^16 < 2^31, so no integer sum overflows.
   double g_bound = 274877906944.0;
+  double g_bound_df = 1180591620717411303424.0;   // double-float path's bound (2^70 at most)
 };
 
 // Parses a potential file; returns false with `err` set on failure.

@@ -19,6 +19,8 @@ from . import build as _build
 PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_MIXED_A64 = 2   # mixed, with the order-parameter sums in plain FP64
+PREC_FP64_NATIVE = 3  # every product and sum in native FP64 (PREC_FP64 runs the
+                      # invariant/adjoint products in double-float arithmetic)
 ERRORS = {1: "EINVAL", 2: "EIO", 3: "ENOMEM", 4: "ECUDA", 5: "ENOTSUP", 6: "ECAPACITY",
           7: "ENOGPU", 8: "ETIMEDOUT", 9: "EBUSY"}
 

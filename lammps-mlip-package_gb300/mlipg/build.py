@@ -57,6 +57,7 @@ def _sources():
         "features.o": ("nvcc", os.path.join(CSRC, "features.cu")),
         "pair.o": ("nvcc", os.path.join(CSRC, "pair.cu")),
         "kernels_f64.o": ("nvcc", os.path.join(CSRC, "kernels_f64.cu")),
+        "kernels_f64df.o": ("nvcc", os.path.join(CSRC, "kernels_f64df.cu")),
         "kernels_f32.o": ("nvcc", os.path.join(CSRC, "kernels_f32.cu")),
     }
 

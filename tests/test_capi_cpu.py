@@ -73,19 +73,20 @@ def test_type_map_semantics(potdir):
 
 
 def test_precision_values(potdir):
-    """The three precisions are accepted at creation and by set_precision;
+    """The four precisions are accepted at creation and by set_precision;
     anything else is EINVAL and leaves the handle as it was."""
-    for prec in (mlipg.PREC_FP64, mlipg.PREC_MIXED, mlipg.PREC_MIXED_A64):
+    for prec in (mlipg.PREC_FP64, mlipg.PREC_MIXED, mlipg.PREC_MIXED_A64,
+                 mlipg.PREC_FP64_NATIVE):
         p = mlipg.Potential(potdir["gtinv-434"], prec)
         p.set_precision(mlipg.PREC_MIXED_A64)
         p.set_precision(prec)
-        for bad in (-1, 3):
+        for bad in (-1, 4):
             with pytest.raises(mlipg.MlipgError) as e:
                 p.set_precision(bad)
             assert e.value.code == 1
         p.close()
     with pytest.raises(mlipg.MlipgError) as e:
-        mlipg.Potential(potdir["gtinv-434"], 3)
+        mlipg.Potential(potdir["gtinv-434"], 4)
     assert e.value.code == 1
 
 

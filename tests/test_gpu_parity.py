@@ -1,9 +1,11 @@
 """GPU path (through the C ABI) against the CPU oracle and the golden logs.
 
 Tolerances:
-* FP64 path: energy, every force component and the virial agree with the
-  oracle to 1e-10 relative (to the largest magnitude of each quantity);
-  only the summation order differs.
+* FP64 precisions: energy, every force component and the virial agree with
+  the oracle to 1e-10 relative (to the largest magnitude of each quantity).
+  MLIPG_PREC_FP64_NATIVE differs from the oracle only in summation order;
+  MLIPG_PREC_FP64 runs the invariant and adjoint products in double-float
+  arithmetic (a few 2^-47 per operation) and agrees to ~1e-13.
 * mixed path: force RMS error <= 1e-4 eV/A against the FP64 oracle on every
   potential.  Energy: the polynomial's input features and their whole
   energy (linear and polynomial terms) are evaluated in FP64, so a potential
@@ -50,12 +52,13 @@ def ref_cache():
     return {}
 
 
+@pytest.mark.parametrize("prec", [mlipg.PREC_FP64, mlipg.PREC_FP64_NATIVE])
 @pytest.mark.parametrize("pot", ["gtinv-197", "gtinv-820", "gtinv-434"])
-def test_regression_potentials_fp64(potdir, golden, pot):
+def test_regression_potentials_fp64(potdir, golden, pot, prec):
     o = Oracle(potdir[pot], threads=16)
     s = build_system(structure("structure.lammps"), o.cutoff, skin=2.0)
     ref = o.compute(s)
-    g = mlipg.Potential(potdir[pot], mlipg.PREC_FP64)
+    g = mlipg.Potential(potdir[pot], prec)
     got = g.compute(s)
     check_fp64(got, ref, s)
     gl = golden["thermo_step0"][pot]

@@ -125,7 +125,8 @@ def test_adjoint_range_bit_everywhere(huge_pot):
     with pytest.raises(mlipg.MlipgError) as ei:
         srv.wait(tk, timeout_ms=60000)
     assert ei.value.code == 5
-    # the FP64 path has no fixed-point range: the same requests succeed
+    # the FP64 path keeps FP64's range (coefficients beyond FP32's range run
+    # the all-FP64 kernel): the same requests succeed
     tk = srv.submit(cell, mlipg.PREC_FP64)
     e, f, v = srv.wait(tk, timeout_ms=60000)
     assert np.isfinite(e)
