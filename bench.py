@@ -12,11 +12,14 @@ Reported (one JSON line on rank 0):
   value      atom-steps/s, inputs resident in HBM (positions, CSR full list)
   e2e        the same through mlipg_compute with LAMMPS-shaped host arrays,
              host->device and device->host copies inside the timed region
-  fp64       the plain FP64 path on a bounded subset of centres of the same
-             structure, and the mixed/FP64 speed ratio
+  fp64       MLIPG_PREC_FP64 (double-float invariant/adjoint products) on all
+             centres of the same structure, and the mixed/FP64 speed ratio
+  fp64_native  the all-FP64 form on a bounded subset of the centres
   accuracy   mixed vs FP64 (GPU) on a 4,000-atom cell of the same workload
   roofline   algorithmic FLOPs per fused-kernel launch / its CUDA-event time,
-             against the live FP32 FMA peak of the device
+             against the live FP32 FMA peak of the device; also on the folded
+             table the kernel executes and against the FP32 pipe's arithmetic
+             rate at the measured clock
   cpu_baseline  the CPU oracle (restatement of the reference algorithm) on a
              bounded sample of centres, all host threads
 `--impl reference` times that CPU implementation alone on the same workload.
@@ -407,27 +410,41 @@ def run_ours(args, dist):
            "d2h_bytes_per_step": int(24 * sysm.nall + 8 * 8 + 4),
            "api": "mlipg_compute (LAMMPS-shaped host arrays)"}
 
-    # ---------------- plain FP64 path on a bounded subset of centres, with
-    # its own tile shape (autotuned for FP64 unless one is fixed)
+    # ---------------- FP64 (MLIPG_PREC_FP64: the invariant/adjoint products in
+    # double-float arithmetic) on all centres, and the all-FP64 form
+    # (MLIPG_PREC_FP64_NATIVE) on a bounded subset of them, with their own
+    # tile shape (autotuned for FP64 unless one is fixed)
     mixed_tiling = g.tiling()
     g.set_precision(mlipg.PREC_FP64)
-    nsub = max(1024, min(natoms, int(natoms * args.fp64_fraction)))
     fp64_tiling = None
     if args.autotune:
-        g.autotune_device(min(nsub, 9728), d_x4.data_ptr(), d_cent.data_ptr(), d_off.data_ptr(),
-                          d_idx.data_ptr(), d_f.data_ptr(), d_out.data_ptr(), nb_cap=nb_cap)
+        g.autotune_device(min(ncent_main, 9728), d_x4.data_ptr(), d_cent.data_ptr(),
+                          d_off.data_ptr(), d_idx.data_ptr(), d_f.data_ptr(), d_out.data_ptr(),
+                          nb_cap=nb_cap)
         fp64_tiling = g.tiling()
-    step(nsub)
-    torch.cuda.synchronize()
-    clocks64 = ClockSampler(0)
-    clocks64.start()
-    ev0.record(stream)
-    for _ in range(2):
-        step(nsub)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    clk64 = clocks64.stop()
-    fp64_v = nsub * 2 / (ev0.elapsed_time(ev1) * 1e-3)
+
+    def timed_launches(ncent, n):
+        step(ncent)
+        torch.cuda.synchronize()
+        g.kernel_times()
+        g.set_profiling(True)
+        ck = ClockSampler(0)
+        ck.start()
+        ev0.record(stream)
+        for _ in range(n):
+            step(ncent)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        c = ck.stop()
+        g.set_profiling(False)
+        kt_ = [t for t in g.kernel_times() if t > 0]
+        return ncent * n / (ev0.elapsed_time(ev1) * 1e-3), c, float(np.mean(kt_)) if kt_ else None
+
+    fp64_v, clk64, kms64 = timed_launches(ncent_main, 2)
+    e_fp64 = float(d_out[0].item())
+    g.set_precision(mlipg.PREC_FP64_NATIVE)
+    nsub = max(1024, min(ncent_main, int(ncent_main * args.fp64_fraction)))
+    nat_v, clk_nat, kms_nat = timed_launches(nsub, 2)
     g.set_precision(mlipg.PREC_MIXED)
     g.set_tiling(mixed_tiling["irr_chunk"], mixed_tiling["warp_order"],
                  mixed_tiling["ctas_per_sm"])
@@ -484,6 +501,19 @@ def run_ours(args, dist):
             # positions+element, centre, CSR offsets and indices read; forces written
             "algorithmic_bytes_per_launch": int(32 * sysm.nall + 8 * natoms + 4 * sysm.npairs +
                                                 24 * sysm.nall)}
+    # the kernels run the folded table (each conjugate pair of terms once):
+    # the same FLOP model on it, and the FP32 pipe's arithmetic rate
+    # (SMs x 128 lanes x 2 FLOP x the SM clock seen during the timed launches)
+    flops_exec = sum(cnt * g.flops_per_atom_step(t, nb, executed=True)
+                     for t, (cnt, nb) in nbar.items())
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    arith = nsm * 128 * 2 * (clk.get("sm_mhz") or 0) * 1e6 / 1e12
+    ach_exec = flops_exec / (kmean * 1e-3) / 1e12
+    roof.update({"executed_flops_per_launch": flops_exec,
+                 "achieved_executed": ach_exec, "frac_executed": ach_exec / peak,
+                 "arith_peak_fp32": arith,
+                 "frac_arith": achieved / arith if arith > 0 else None,
+                 "frac_executed_arith": ach_exec / arith if arith > 0 else None})
     roof.update(profiled_traffic(args.workload))
 
     if rank == 0:
@@ -504,8 +534,16 @@ def run_ours(args, dist):
                            "step": "energy + forces + virial of all atoms, one fused launch",
                            "tiling": tune},
                 "e2e": e2e,
-                "fp64": {"value": fp64_v, "unit": UNIT, "centres": nsub, "tiling": fp64_tiling,
+                "fp64": {"value": fp64_v, "unit": UNIT, "centres": ncent_main,
+                         "what": "MLIPG_PREC_FP64: FP64 order parameters, polynomial, forces; "
+                                 "invariant/adjoint products in double-float arithmetic, "
+                                 "adjoint in exact fixed point",
+                         "kernel_ms": kms64, "energy_eV": e_fp64, "tiling": fp64_tiling,
                          "mixed_over_fp64": value / dist["world"] / fp64_v, "clocks": clk64},
+                "fp64_native": {"value": nat_v, "unit": UNIT, "centres": nsub,
+                                "what": "MLIPG_PREC_FP64_NATIVE: every product and sum in FP64",
+                                "kernel_ms": kms_nat,
+                                "fp64_over_native": fp64_v / nat_v, "clocks": clk_nat},
                 "mixed_a64": {"value": a64_v, "unit": UNIT,
                               "what": "MLIPG_PREC_MIXED_A64: order-parameter sums in plain FP64",
                               "accuracy_vs_fp64": acc_a64},
@@ -799,20 +837,21 @@ def serve_record(args, dist, workload):
     atoms = int(sum(pool[pick[k]].natoms for k in range(nreq)))
     # roofline: algorithmic FLOPs of every served atom-step (counting rule of
     # the fused kernel, per element at the pool's mean neighbour count) over
-    # the wall time of the stream, against the FP32 FMA peak; FP64 requests
-    # run on the 64x narrower FP64 pipe, so their FLOPs are also reported apart
+    # the wall time of the stream, against the FP32 FMA peak (FP64 requests
+    # run their invariant/adjoint products in double-float arithmetic on the
+    # FP32 pipe, about 15 FP32 operations per FP64-class FMA, so their FLOPs
+    # are also reported apart)
     g = mlipg.Potential(pot, mlipg.PREC_MIXED)
     nb_mean = 4.18879 * 6.0 ** 3 * spec["density"]
     fl = np.array([sum(int(np.sum(pool[pick[k]].types == t)) * g.flops_per_atom_step(int(t), nb_mean)
                        for t in range(spec["ntypes"])) for k in range(nreq)])
     g.close()
     peak = mlipg.measure_fma_peak(False)
-    peak64 = mlipg.measure_fma_peak(True)
     ach = fl.sum() / el / 1e12
-    roof = {"bound": "fp32-cuda-core (mixed requests) / fp64 (FP64 requests)", "achieved": ach,
+    roof = {"bound": "fp32-cuda-core (mixed requests: FP32 products; FP64 requests: "
+                     "double-float products)", "achieved": ach,
             "peak": peak, "unit": "TFLOP/s", "frac": ach / peak, "traffic": None,
             "fp64_share_of_flops": float(fl[prec == mlipg.PREC_FP64].sum() / fl.sum()),
-            "fp64_peak": peak64,
             "note": "whole-stream average at %.0f%% offered load (the GPU idles between "
                     "arrivals)" % (100 * spec["load"])}
     if rank == 0:

@@ -190,8 +190,12 @@ int mlipg_model_info(const mlipg_handle* h, long long* out13);
 long mlipg_dump_itc(const mlipg_handle* h, int* out, long cap);
 long mlipg_dump_poly(const mlipg_handle* h, int* out, long cap);
 
-/* Algorithmic FLOPs per atom step for element `elem` with nbar neighbours. */
+/* Algorithmic FLOPs per atom step for element `elem` with nbar neighbours
+ * (invariants and adjoint counted on the raw coupling table), and the same
+ * count on the folded table the kernels execute (each conjugate pair of
+ * terms once).  Measurement support; no reference counterpart. */
 double mlipg_flops_per_atom_step(const mlipg_handle* h, int elem, double nbar);
+double mlipg_flops_per_atom_step_executed(const mlipg_handle* h, int elem, double nbar);
 
 /* Per-launch device time of the fused kernel: when on, every launch is
  * bracketed by CUDA events on the handle's stream; mlipg_kernel_times copies

@@ -95,6 +95,7 @@ struct mlipg_handle {
   double rec_q = 0.0;
   // per-call buffers (grow only)
   DevBuf d_x4, d_centers, d_off, d_idx, d_f, d_eatom, d_vatom, d_partials, d_status, d_out8;
+  DevBuf d_gexp;   // [2][kMaxTypes] adapted fixed-point exponents (mixed, double-float)
   HostBuf h_x4, h_centers, h_off, h_idx, h_f, h_eatom, h_out;
   int last_status = 0;
   const int* last_status_dev = nullptr;   // status word of the last launch (device)
@@ -240,6 +241,7 @@ static int upload_model(mlipg_handle* h) {
     CK(upload(h->d_wlin_df, wd, s), "upload linear weights (double-float)");
   }
   CK(upload(h->d_radial, radial, s), "upload radial parameters");
+  CK(upload(h->d_gexp, std::vector<int>(2 * kMaxTypes, 0), s), "upload scale exponents");
   if (M.pot.pair) {
     CK(upload(h->d_pair_terms, M.pair_terms, s), "upload pair terms");
     CK(upload(h->d_pair_term_off, M.pair_term_off, s), "upload pair term offsets");
@@ -351,7 +353,7 @@ int mlipg_destroy(mlipg_handle* h) {
                     &h->d_type_pairs,
                     &h->d_x4,
                     &h->d_centers, &h->d_off, &h->d_idx, &h->d_f, &h->d_eatom, &h->d_vatom, &h->d_partials,
-                    &h->d_status, &h->d_out8};
+                    &h->d_status, &h->d_out8, &h->d_gexp};
   for (DevBuf* b : bufs) b->release();
   for (auto& pr : h->ev_pending) h->ev_pool.insert(h->ev_pool.end(), {pr.first, pr.second});
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
@@ -567,6 +569,8 @@ static int launch_eval(mlipg_handle* h, int ncenters, const double4* x4, const i
   a.nl_cap = std::max(M.max_nl, 1);
   a.rc = M.pot.cutoff;
   a.g_bound = (float)(var == kVariantF64DF ? M.g_bound_df : M.g_bound);
+  a.gexp_cache = var == kVariantF64 ? nullptr
+                                    : h->d_gexp.as<int>() + (var == kVariantF64DF ? kMaxTypes : 0);
   a.unit_dyn = M.tiling.warp_order == 2 ? 1 : 0;
   a.sum64 = h->precision == MLIPG_PREC_MIXED_A64 ? 1 : 0;
   a.lh64 = var == kVariantF32 ? M.lh64 : 0;
@@ -860,6 +864,12 @@ extern "C" long mlipg_dump_poly(const mlipg_handle* h, int* out, long cap) {
 extern "C" double mlipg_flops_per_atom_step(const mlipg_handle* h, int elem, double nbar) {
   if (!h || elem < 0 || elem >= h->model.T) return 0.0;
   return flops_per_atom_step(h->model, elem, nbar);
+}
+
+extern "C" double mlipg_flops_per_atom_step_executed(const mlipg_handle* h, int elem,
+                                                     double nbar) {
+  if (!h || elem < 0 || elem >= h->model.T) return 0.0;
+  return flops_per_atom_step(h->model, elem, nbar, true);
 }
 
 

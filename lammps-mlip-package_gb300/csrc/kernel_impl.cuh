@@ -1053,12 +1053,32 @@ __device__ __forceinline__ DF pick(int z, const DF (&v)[N]) {
   return r;
 }
 
-// Double-float form of run_irr (same algebra, same flushes).  The element
-// loop over slot z is kept rolled (the operands of the current z are picked
-// from registers by selects): fully unrolled, the double-float body of one
-// term outgrows the instruction cache and the warps wait on instruction
-// fetch.  Sums go through DFA accumulators (one FP32 add of dependency per
-// accumulation), products of accumulated values are renormalised once.
+template <int N>
+__device__ __forceinline__ DFA pick_acc(int i, const DFA (&v)[N]) {
+  DFA r = v[0];
+#pragma unroll
+  for (int k = 1; k < N; ++k) {
+    r.s = (i == k) ? v[k].s : r.s;
+    r.c = (i == k) ? v[k].c : r.c;
+  }
+  return r;
+}
+template <int N>
+__device__ __forceinline__ void put_acc(int i, DFA (&v)[N], const DFA& x) {
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    v[k].s = (i == k) ? x.s : v[k].s;
+    v[k].c = (i == k) ? x.c : v[k].c;
+  }
+}
+
+// Double-float form of run_irr (same sums, same flushes).  The loop over
+// the (z, x) element pairs is kept rolled (the operands of the current pair
+// are picked from registers by selects): fully unrolled, the double-float
+// body of one term outgrows the instruction cache and the warps wait on
+// instruction fetch.  Sums go through DFA accumulators (one FP32 add of
+// dependency per accumulation); accumulated values that are multiplied
+// again are renormalised once.
 template <int Q, int TT, int Lh, class EA>
 __device__ __forceinline__ void run_irr_df(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                            const DeviceTerm* __restrict__ terms,
@@ -1071,13 +1091,13 @@ __device__ __forceinline__ void run_irr_df(const DeviceIrrUnit& u, const DeviceT
   constexpr int PZ = (Q >= 3) ? Q - 3 : 0;   // slot indices
   constexpr int PX = (Q == 1) ? 0 : Q - 2;
   constexpr int PY = Q - 1;
-  DF H[NZ][NX * NY];
+  DF H[NZ * NX][NY];   // weights of the tuple (z, x, y) at H[z NX + x][y]
 #pragma unroll
-  for (int z = 0; z < NZ; ++z)
+  for (int zx = 0; zx < NZ * NX; ++zx)
 #pragma unroll
-    for (int j = 0; j < NX * NY; ++j) {
-      const int2 e = __ldg(reinterpret_cast<const int2*>(tups + u.tup + z * NX * NY + j));
-      H[z][j] = tuple_weight(e, wlin, hnl, n, act);
+    for (int y = 0; y < NY; ++y) {
+      const int2 e = __ldg(reinterpret_cast<const int2*>(tups + u.tup + zx * NY + y));
+      H[zx][y] = tuple_weight(e, wlin, hnl, n, act);
     }
   const int s0 = (int)u.s0;
   constexpr int es = Lh * kNPad;                // element stride in the a / G arrays
@@ -1139,75 +1159,78 @@ __device__ __forceinline__ void run_irr_df(const DeviceIrrUnit& u, const DeviceT
       cr[0] = DF(1.0f);
       ci[0] = DF(0.0f);
     }
-    DFA Sr, Si, gxr[NX], gxi[NX], gyr[NY], gyi[NY];
-    DF gzr[NZ], gzi[NZ];
-#pragma unroll
-    for (int z = 0; z < NZ; ++z) { gzr[z] = DF(0.0f); gzi[z] = DF(0.0f); }
+    // Rolled loop over the (z, x) element pairs, with m = sum_y H c_y:
+    //   S_z += b_x m,  G_x += a_z m,  G_y += H (a_z b_x)
+    // (S = sum_z a_z S_z afterwards); accumulators of the running z or x
+    // are picked and written back by selects.
+    DFA gzr[NZ], gzi[NZ], gxr[NX], gxi[NX], gyr[NY], gyi[NY];
 #pragma unroll 1
-    for (int z = 0; z < NZ; ++z) {
-      DF Hc[NX * NY];
+    for (int zx = 0; zx < NZ * NX; ++zx) {
+      const int z = zx / NX, x = zx - (zx / NX) * NX;
+      DF hz[NY];
 #pragma unroll
-      for (int j = 0; j < NX * NY; ++j) {
-        Hc[j] = H[0][j];
+      for (int y = 0; y < NY; ++y) {
+        hz[y] = H[0][y];
 #pragma unroll
-        for (int q = 1; q < NZ; ++q) Hc[j] = (z == q) ? H[q][j] : Hc[j];
+        for (int q = 1; q < NZ * NX; ++q) hz[y] = (zx == q) ? H[q][y] : hz[y];
       }
-      const DF ar = pick(z, zr), ai = pick(z, zi);
-      // m[x] = sum_y H c[y]
-      DF mr[NX], mi[NX];
-#pragma unroll
-      for (int x = 0; x < NX; ++x) {
-        if (Q == 1) {
-          mr[x] = Hc[x];
-          mi[x] = DF(0.0f);
-        } else {
-          DFA tr, ti;
-#pragma unroll
-          for (int y = 0; y < NY; ++y) {
-            acc_fma(tr, Hc[x * NY + y], cr[y]);
-            acc_fma(ti, Hc[x * NY + y], ci[y]);
-          }
-          mr[x] = acc_val(tr);
-          mi[x] = acc_val(ti);
-        }
-      }
-      // S_z = sum_x b[x] m[x]
-      DFA szr, szi;
-#pragma unroll
-      for (int x = 0; x < NX; ++x) cacc(szr, szi, br[x], bi[x], mr[x], mi[x]);
-      const DF sr = acc_val(szr), si = acc_val(szi);
-      if (Q >= 3) {
-#pragma unroll
-        for (int q = 0; q < NZ; ++q) {
-          gzr[q] = (z == q) ? sr : gzr[q];
-          gzi[q] = (z == q) ? si : gzi[q];
-        }
-        cacc(Sr, Si, ar, ai, sr, si);
-#pragma unroll
-        for (int x = 0; x < NX; ++x) cacc(gxr[x], gxi[x], ar, ai, mr[x], mi[x]);
+      const DF bxr = pick(x, br), bxi = pick(x, bi);
+      DF mr, mi;
+      if (Q == 1) {
+        mr = hz[0];
+        mi = DF(0.0f);
       } else {
-        acc_add(Sr, sr);
-        acc_add(Si, si);
-#pragma unroll
-        for (int x = 0; x < NX; ++x) { acc_add(gxr[x], mr[x]); acc_add(gxi[x], mi[x]); }
-      }
-      if (Q > 1) {
+        DFA tr, ti;
 #pragma unroll
         for (int y = 0; y < NY; ++y) {
-          DFA tr, ti;
+          acc_fma(tr, hz[y], cr[y]);
+          acc_fma(ti, hz[y], ci[y]);
+        }
+        mr = acc_val(tr);
+        mi = acc_val(ti);
+      }
+      {
+        DFA tr = pick_acc(z, gzr), ti = pick_acc(z, gzi);
+        cacc(tr, ti, bxr, bxi, mr, mi);
+        put_acc(z, gzr, tr);
+        put_acc(z, gzi, ti);
+      }
+      DFA ur = pick_acc(x, gxr), ui = pick_acc(x, gxi);
+      if (Q >= 3) {
+        const DF ar = pick(z, zr), ai = pick(z, zi);
+        cacc(ur, ui, ar, ai, mr, mi);
+        if (Q > 1) {
+          DFA pr, pi;
+          cacc(pr, pi, ar, ai, bxr, bxi);
+          const DF Pr = acc_val(pr), Pi = acc_val(pi);
 #pragma unroll
-          for (int x = 0; x < NX; ++x) {
-            acc_fma(tr, Hc[x * NY + y], br[x]);
-            acc_fma(ti, Hc[x * NY + y], bi[x]);
+          for (int y = 0; y < NY; ++y) {
+            acc_fma(gyr[y], hz[y], Pr);
+            acc_fma(gyi[y], hz[y], Pi);
           }
-          if (Q >= 3) {
-            cacc(gyr[y], gyi[y], ar, ai, acc_val(tr), acc_val(ti));
-          } else {
-            gyr[y] = tr;
-            gyi[y] = ti;
+        }
+      } else {
+        acc_add(ur, mr);
+        acc_add(ui, mi);
+        if (Q > 1) {
+#pragma unroll
+          for (int y = 0; y < NY; ++y) {
+            acc_fma(gyr[y], hz[y], bxr);
+            acc_fma(gyi[y], hz[y], bxi);
           }
         }
       }
+      put_acc(x, gxr, ur);
+      put_acc(x, gxi, ui);
+    }
+    DF gzv_r[NZ], gzv_i[NZ];
+    DFA Sr, Si;
+#pragma unroll
+    for (int z = 0; z < NZ; ++z) {
+      gzv_r[z] = acc_val(gzr[z]);
+      gzv_i[z] = acc_val(gzi[z]);
+      if (Q >= 3) cacc(Sr, Si, zr[z], zi[z], gzv_r[z], gzv_i[z]);
+      else { acc_add(Sr, gzv_r[z]); acc_add(Si, gzv_i[z]); }
     }
     const DF Sv = acc_val(Sr), Siv = acc_val(Si);
     const DF ce = self ? c : DF(2.0f) * c;
@@ -1217,11 +1240,11 @@ __device__ __forceinline__ void run_irr_df(const DeviceIrrUnit& u, const DeviceT
       // code; unconditional (lanes n >= F and unused imaginary parts add
       // exact zeros)
       const DF cs = gscale(c, gf);
-      const auto flush = [&](int p, int e, DF vr, DF vi) {
+      const auto flush = [&](int p, int lop, int e, DF vr, DF vi) {
         const unsigned cd = (code >> (2 * p)) & 3u;
         const DF kr = (cd == (unsigned)kSlotMZero) ? DF(2.0f) * cs : cs;
         const DF ki = (cd == 0u) ? cs : (cd == 1u ? -cs : DF(0.0f));
-        int* gp = sg + e * es + lo[p];
+        int* gp = sg + e * es + lop;
         if (Q == 4) {
           gput(gp, kr * (Ar * vr - Ai * vi), gf, kLo);
           gput(gp + kIm, ki * (Ar * vi + Ai * vr), gf, kLo);
@@ -1230,11 +1253,20 @@ __device__ __forceinline__ void run_irr_df(const DeviceIrrUnit& u, const DeviceT
           gput(gp + kIm, ki * vi, gf, kLo);
         }
       };
+      // one rolled loop over the (slot, element) pairs of x and y, the
+      // values picked by selects (code size: see above)
+      constexpr int NW = NX + (Q > 1 ? NY : 0);
+      DF wr[NW], wi[NW];
 #pragma unroll
-      for (int x = 0; x < NX; ++x) flush(PX, x, acc_val(gxr[x]), acc_val(gxi[x]));
+      for (int x = 0; x < NX; ++x) { wr[x] = acc_val(gxr[x]); wi[x] = acc_val(gxi[x]); }
       if (Q > 1) {
 #pragma unroll
-        for (int y = 0; y < NY; ++y) flush(PY, y, acc_val(gyr[y]), acc_val(gyi[y]));
+        for (int y = 0; y < NY; ++y) { wr[NX + y] = acc_val(gyr[y]); wi[NX + y] = acc_val(gyi[y]); }
+      }
+#pragma unroll 1
+      for (int w = 0; w < NW; ++w) {
+        const bool isx = w < NX;
+        flush(isx ? PX : PY, isx ? lo[PX] : lo[PY], isx ? w : w - NX, pick(w, wr), pick(w, wi));
       }
     }
     if (Q >= 3) {   // slot z: A S_z, accumulated over the run
@@ -1245,11 +1277,11 @@ __device__ __forceinline__ void run_irr_df(const DeviceIrrUnit& u, const DeviceT
 #pragma unroll
       for (int z = 0; z < NZ; ++z) {
         if (Q == 4) {
-          azr[z] += kr * (Ar * gzr[z] - Ai * gzi[z]);
-          azi[z] += ki * (Ar * gzi[z] + Ai * gzr[z]);
+          azr[z] += kr * (Ar * gzv_r[z] - Ai * gzv_i[z]);
+          azi[z] += ki * (Ar * gzv_i[z] + Ai * gzv_r[z]);
         } else {
-          azr[z] += kr * gzr[z];
-          azi[z] += ki * gzi[z];
+          azr[z] += kr * gzv_r[z];
+          azi[z] += ki * gzv_i[z];
         }
       }
       const bool need = last || ((((unsigned)nxt.z ^ lw) >> (8 * PZ)) & 255u) != 0u;
@@ -1361,6 +1393,183 @@ __device__ __forceinline__ void radial64(const KernelArgs& A, double r, double* 
         fv = exp(-beta * dr * dr) * fc;
       }
       f[n] = fv;
+    }
+  }
+}
+
+// FP64 radial functions and their derivatives for all 16 channels (P6 of
+// the FP64 kernels): the Gaussians g_n by the recurrence of radial64 when
+// beta is common, f_n = g_n fc, f'_n = -2 beta (r - mu_n) g_n fc + g_n fc'.
+__device__ __forceinline__ void radial64d(const KernelArgs& A, double r, double* f, double* fd) {
+  double sn, cs;
+  sincospi(r / A.rc, &sn, &cs);
+  const bool in = r < A.rc;
+  const double fc = in ? 0.5 * (cs + 1.0) : 0.0;
+  const double fcd = in ? -0.5 * 3.14159265358979323846 / A.rc * sn : 0.0;
+  const int F = A.F;
+  if (A.radial_rec) {
+    const double beta = __ldg(A.radial), mu0 = __ldg(A.radial + 1);
+    const double q = exp(A.rec_q * r);
+    double g = exp(-beta * (r - mu0) * (r - mu0));
+#pragma unroll
+    for (int n = 0; n < kNPad; ++n) {
+      const double mu = n < F ? __ldg(A.radial + 2 * n + 1) : 0.0;
+      f[n] = n < F ? g * fc : 0.0;
+      fd[n] = n < F ? (-2.0 * beta * (r - mu) * g) * fc + g * fcd : 0.0;
+      if (n + 1 < F) {
+        const double2 ke = __ldg(reinterpret_cast<const double2*>(A.radial_rec) + n);
+        g = g * q * ke.x * fma(ke.y, r, 1.0);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int n = 0; n < kNPad; ++n) {
+      f[n] = 0.0;
+      fd[n] = 0.0;
+      if (n < F) {
+        const double beta = __ldg(A.radial + 2 * n), dr = r - __ldg(A.radial + 2 * n + 1);
+        const double g = exp(-beta * dr * dr);
+        f[n] = g * fc;
+        fd[n] = (-2.0 * beta * dr * g) * fc + g * fcd;
+      }
+    }
+  }
+}
+
+// Force contributions of one neighbour at one (l, m <= 0) for all 16
+// channels (P6 of the FP64 kernels): with G of the neighbour's element row,
+// g0 = sum_n f_n G_n, g1 = sum_n f'_n G_n, and the same force expression as
+// ForceVis.
+struct ForceVis16 {
+  const double* g;   // Re G of the neighbour's element slot, channel 0: [Lh][16]; Im at g + gim
+  int gim;
+  const double* f;
+  const double* fd;
+  double ux, uy, uz;
+  double fx, fy, fz;
+  __device__ __forceinline__ void operator()(int lmh, int mp, double yre, double yim, double xre,
+                                             double xim, double yyre, double yyim, double zre,
+                                             double zim) {
+    double g0r = 0, g0i = 0, g1r = 0, g1i = 0;
+#pragma unroll
+    for (int q = 0; q < kNPad; q += 4) {
+      double gr[4], gi[4];
+      load4(g + lmh * kNPad + q, gr);
+      load4(g + gim + lmh * kNPad + q, gi);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        g0r = fma(f[q + k], gr[k], g0r);
+        g0i = fma(f[q + k], gi[k], g0i);
+        g1r = fma(fd[q + k], gr[k], g1r);
+        g1i = fma(fd[q + k], gi[k], g1i);
+      }
+    }
+    const double coeff = (mp == 0) ? 1.0 : 2.0;
+    const double ry = yre * g1r + yim * g1i;
+    fx += coeff * (ry * ux + (xre * g0r + xim * g0i));
+    fy += coeff * (ry * uy + (yyre * g0r + yyim * g0i));
+    fz += coeff * (ry * uz + (zre * g0r + zim * g0i));
+  }
+};
+
+// Column set of the FP64 force phase: column m goes to part
+// (0 1 2 3 3 2 1 0 0 1 ...)[m] of the four, which balances the columns'
+// lengths (L - m + 1 entries each).
+__device__ __forceinline__ int column_part(int mp) {
+  const int s = mp & 7;
+  return s < 4 ? s : 7 - s;
+}
+
+// sh_visit (FP64, with derivatives) restricted to the columns m of one part:
+// every column still advances the cheap Q recursion that the next column's
+// derivatives read, and the angle recursions; P, Y, dY and the visitor run
+// for the part's own columns only.  `part` is uniform across the warp.
+template <int LCAP, typename V>
+__device__ __forceinline__ void sh_visit_part(double dx, double dy, double dz, double r, int L,
+                                              int part, V& vis) {
+  const double invr = 1.0 / r;
+  const double ct = dz * invr;
+  const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+  const double rho2 = dx * dx + dy * dy;
+  double cp = 1.0, sp = 0.0;
+  if (rho2 > 0.0) {
+    const double ir = 1.0 / sqrt(rho2);
+    cp = dx * ir;
+    sp = dy * ir;
+  }
+  const double h = 0.70710678118654752440;   // 0.5 * sqrt(2)
+  double Qc[LCAP + 2];
+#pragma unroll
+  for (int l = 0; l < LCAP + 2; ++l) Qc[l] = 0.0;
+  double pdiag = 0.39894228040143267794;      // P_0^0 = sqrt(1/(2 pi))
+  double cm = 1.0, sm = 0.0, cprev = cp, sprev = -sp;
+  const double tc = 2.0 * cp;
+  double sgn = 1.0;
+#pragma unroll
+  for (int mp = 0; mp <= LCAP; ++mp) {
+    if (mp > L) break;
+    if (mp > 0) {
+      const double s = tc * sm - sprev;
+      const double c = tc * cm - cprev;
+      cprev = cm; cm = c; sprev = sm; sm = s;
+      pdiag = pdiag * ((double)cDiag[mp] * st);
+      sgn = -sgn;
+    }
+    const bool mine = column_part(mp) == part;
+    const double qn_diag = (mp == 0) ? -0.48860251190291992263 : Qc[mp] * ((double)cDiag[mp + 1] * st);
+    double p1 = 0.0, p2 = 0.0, qn1 = 0.0, qn2 = 0.0;
+#pragma unroll
+    for (int l = mp; l <= LCAP; ++l) {
+      if (l > L) break;
+      double Qn = 0.0;
+      if (l == mp + 1) Qn = qn_diag;
+      else if (l == mp + 2) Qn = (ct * (double)cOff[mp + 1]) * qn1;
+      else if (l >= mp + 3) Qn = (double)cA[lm2i(l, mp + 1)] * (ct * qn1 + (double)cB[lm2i(l, mp + 1)] * qn2);
+      if (l >= mp + 1) { qn2 = qn1; qn1 = Qn; }
+      if (mine) {
+        double P;
+        if (l == mp) P = pdiag;
+        else if (l == mp + 1) P = (ct * (double)cOff[mp]) * p1;
+        else P = (double)cA[lm2i(l, mp)] * (ct * p1 + (double)cB[lm2i(l, mp)] * p2);
+        p2 = p1;
+        p1 = P;
+        double yre, yim;
+        if (mp == 0) {
+          yre = P * h;
+          yim = 0.0;
+        } else {
+          const double t = sgn * P * h;
+          yre = t * cm;
+          yim = -(t * sm);
+        }
+        const int lmh = l * (l + 1) / 2 + l - mp;
+        double xre = 0, xim = 0, yyre = 0, yyim = 0, zre = 0, zim = 0;
+        if (mp == 0) {
+          if (l >= 1) {
+            const double common = Qn * st * invr * (double)cLL[l];
+            xre = common * ct * cp;
+            yyre = common * ct * sp;
+            zre = -common * st;
+          }
+        } else {
+          const double qc = Qc[l];
+          double dth = (double)mp * ct * qc;
+          if (l != mp) dth += (double)cLM[lm2i(l, mp)] * Qn * st;
+          const double dph = (double)mp * qc;
+          const double ere = cm * h * invr, eim = sm * h * invr;
+          const double vxr = dth * ct * cp, vxi = -dph * sp;
+          const double vyr = dth * ct * sp, vyi = dph * cp;
+          const double vzr = -dth * st;
+          xre = sgn * (ere * vxr - eim * vxi);
+          xim = -sgn * (ere * vxi + eim * vxr);
+          yyre = sgn * (ere * vyr - eim * vyi);
+          yyim = -sgn * (ere * vyi + eim * vyr);
+          zre = sgn * (ere * vzr);
+          zim = -sgn * (eim * vzr);
+        }
+        vis(lmh, mp, yre, yim, xre, xim, yyre, yyim, zre, zim);
+      }
+      if (l >= mp + 1) Qc[l] = Qn;
     }
   }
 }
@@ -1554,9 +1763,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     tstamp = t_;                                \
   }
 
-  // mixed path: fixed-point exponent of the adjoint per centre element
-  // (adapted from centre to centre; the first centre of an element adjusts it)
-  if (tid < kMaxTypes) misc[16 + tid] = 0;
+  // fixed-point paths: exponent of the adjoint's scale per centre element,
+  // adapted from centre to centre (a centre whose flushes leave the range,
+  // or use too little of it, is redone at the adapted scale); it starts from
+  // the handle's cache of the values a previous launch ended with, so short
+  // launches (small cells, MD steps) do not pay the adaptation again
+  if (tid < kMaxTypes) misc[16 + tid] = A.gexp_cache ? A.gexp_cache[tid] : 0;
   __syncthreads();
   for (int c = blockIdx.x; c < A.ncenters; c += gridDim.x) {
     const int i = __ldg(A.centers + c);
@@ -2052,7 +2264,55 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     // ---------------------------------------------------------------- P6
     double fix = 0.0, fiy = 0.0, fiz = 0.0;
     double va[6] = {0, 0, 0, 0, 0, 0};   // this centre's virial (reference order)
-    {
+    if constexpr (sizeof(R) == 8) {
+      // FP64 kernels: 32 neighbours per warp, the four warps of a group split
+      // the m columns of the harmonics (each Y_lm and dY_lm computed once, all
+      // 16 channels contracted per entry); the four partial forces of a
+      // neighbour meet in shared memory (the space of a in the all-FP64
+      // kernel, of the adjoint words in the double-float one: neither is read
+      // again for this centre) and are added in a fixed order.
+      double* pf = reinterpret_cast<double*>(kDF ? static_cast<void*>(sg) : static_cast<void*>(sa));
+      const int part = warp & 3, grp = warp >> 2;
+      const int rounds = (nkeep + 2 * 32 - 1) / (2 * 32);
+      for (int it = 0; it < rounds; ++it) {
+        const int jj = it * 64 + grp * 32 + lane;
+        const bool valid = jj < nkeep;
+        const int k = valid ? nbk[jj] : nbk[0];
+        const int j = __ldg(A.nbr_idx + k);
+        const double4 xj = A.x4[j];
+        const int tj = valid ? (int)xj.w : 0;
+        double dx, dy, dz;
+        pair_disp(A, c, k, xi, xj, dx, dy, dz);
+        if (!valid) { dx = 1.0; dy = 0.0; dz = 0.0; }
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        double f[kNPad], fd[kNPad];
+        radial64d(A, r, f, fd);
+        const double ir = 1.0 / r;
+        ForceVis16 v{reinterpret_cast<const double*>(gP6) + (size_t)tj * LS * kNPad, gim, f, fd,
+                     dx * ir, dy * ir, dz * ir, 0.0, 0.0, 0.0};
+        sh_visit_part<LCAP>(dx, dy, dz, r, L, part, v);
+        double* q = pf + ((grp * 32 + lane) * 4 + part) * 3;
+        q[0] = v.fx;
+        q[1] = v.fy;
+        q[2] = v.fz;
+        __syncthreads();
+        if (part == 0 && valid) {
+          const double* q0 = pf + (grp * 32 + lane) * 12;
+          const double fx = (q0[0] + q0[3]) + (q0[6] + q0[9]);
+          const double fy = (q0[1] + q0[4]) + (q0[7] + q0[10]);
+          const double fz = (q0[2] + q0[5]) + (q0[8] + q0[11]);
+          fix += fx; fiy += fy; fiz += fz;
+          const int fj = A.fold ? __ldg(A.fold + j) : j;
+          atomicAdd(A.f + 3 * (size_t)fj, -fx);
+          atomicAdd(A.f + 3 * (size_t)fj + 1, -fy);
+          atomicAdd(A.f + 3 * (size_t)fj + 2, -fz);
+          // reference component order: xx yy zz yz zx xy
+          va[0] -= dx * fx; va[1] -= dy * fy; va[2] -= dz * fz;
+          va[3] -= dy * fz; va[4] -= dz * fx; va[5] -= dx * fy;
+        }
+        __syncthreads();
+      }
+    } else {
       // 4 threads per neighbour; thread `sub` owns radial channels 4*sub..4*sub+3
       const int sub = tid & 3, n0 = 4 * sub;
       const int rounds = (nkeep + kBlock / 4 - 1) / (kBlock / 4);
@@ -2128,6 +2388,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
 #undef MLIPG_STAMP
   if (prof && tid == 0)
     for (int k = 0; k < 6; ++k) atomicAdd(A.phase_clocks + k, ph[k]);
+  // CTA 0 leaves its adapted exponents for the next launch (any recent value
+  // is a good start; the cache only saves redone centres)
+  if (kFixG && blockIdx.x == 0 && tid < T && A.gexp_cache) A.gexp_cache[tid] = misc[16 + tid];
   // per-CTA partial sums: energy + virial (reference order)
   double vals[7] = {ecta, vir[0], vir[1], vir[2], vir[3], vir[4], vir[5]};
 #pragma unroll

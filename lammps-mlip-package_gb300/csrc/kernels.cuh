@@ -64,6 +64,7 @@ struct KernelArgs {
   int T, F, L, Lh, nb_cap, nl_cap;
   double rc;
   float g_bound;          // fixed-point paths: largest adjoint flush (power of two)
+  int* gexp_cache;        // fixed-point paths: [kMaxTypes] scale exponents to start from
   int unit_dyn;           // 1: warps take batched units from a shared counter
   int sum64;              // mixed path: order-parameter sums in plain FP64 FMAs
   int lh64;               // mixed path: rows of FP64 order parameters (0 = none)

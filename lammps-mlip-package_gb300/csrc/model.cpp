@@ -947,7 +947,7 @@ bool count_coefficients(int n_types, int model_type, int maxp, int maxl, int gti
   return true;
 }
 
-double flops_per_atom_step(const Model& M, int t, double nbar) {
+double flops_per_atom_step(const Model& M, int t, double nbar, bool folded) {
   if (M.pot.pair) {
     // radial-only descriptor: per neighbour and radial function the feature
     // sum (1) and the force contraction (2 + 3); the polynomial and its
@@ -963,7 +963,7 @@ double flops_per_atom_step(const Model& M, int t, double nbar) {
   for (int i = 0; i < M.n_itc; ++i) {
     if (!M.itc[i].inter[t]) continue;
     const int k = M.itc[i].irreps;
-    const double Ti = M.irr_nterms[k];
+    const double Ti = folded ? M.irr_cnterms[k] : M.irr_nterms[k];
     const int q = (int)M.irr_l[k].size();
     f += M.F * Ti * (6.0 * (q - 1) + 3.0);
     f += M.F * Ti * q * (6.0 * std::max(q - 2, 0) + 4.0);

@@ -201,6 +201,8 @@ bool count_coefficients(int n_types, int model_type, int maxp, int maxl, int gti
 // neighbours inside the cutoff (counting rule: complex*complex 6,
 // real*complex 2, complex add 2, real fma 2; transcendentals and
 // recomputation excluded).
-double flops_per_atom_step(const Model& m, int elem, double nbar);
+// folded: count the invariant/adjoint work on the folded table (each
+// conjugate pair of terms once, as the kernels run it) instead of the raw one
+double flops_per_atom_step(const Model& m, int elem, double nbar, bool folded = false);
 
 }  // namespace mlipg

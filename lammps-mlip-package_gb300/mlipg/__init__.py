@@ -67,6 +67,7 @@ def lib():
         "mlipg_dump_itc": (ctypes.c_long, [P, ip, ctypes.c_long]),
         "mlipg_dump_poly": (ctypes.c_long, [P, ip, ctypes.c_long]),
         "mlipg_flops_per_atom_step": (ctypes.c_double, [P, i32, ctypes.c_double]),
+        "mlipg_flops_per_atom_step_executed": (ctypes.c_double, [P, i32, ctypes.c_double]),
         "mlipg_nlist_build": (i32, [dp, i32, dp, ip, ctypes.c_double, ctypes.POINTER(P)]),
         "mlipg_nlist_sizes": (i32, [P, ip, llp]),
         "mlipg_nlist_copy": (i32, [P, dp, ip, ip, ip, ip, ip]),
@@ -250,8 +251,10 @@ class Potential:
         lib().mlipg_dump_poly(self.h, _ip(b), n)
         return b
 
-    def flops_per_atom_step(self, elem: int, nbar: float) -> float:
-        return lib().mlipg_flops_per_atom_step(self.h, elem, nbar)
+    def flops_per_atom_step(self, elem: int, nbar: float, executed: bool = False) -> float:
+        fn = lib().mlipg_flops_per_atom_step_executed if executed else \
+            lib().mlipg_flops_per_atom_step
+        return fn(self.h, elem, nbar)
 
     def compute_lammps(self, nlocal, nall, x, lmp_type, ilist, numneigh, firstneigh_arrays,
                        eatom=True, vatom=False):
