@@ -443,7 +443,9 @@ def run_ours(args, dist):
     fp64_v, clk64, kms64 = timed_launches(ncent_main, 2)
     e_fp64 = float(d_out[0].item())
     g.set_precision(mlipg.PREC_FP64_NATIVE)
-    nsub = max(1024, min(ncent_main, int(ncent_main * args.fp64_fraction)))
+    # a bounded subset (at least 1,024 centres when there are that many; never
+    # more centres than the workload has)
+    nsub = min(ncent_main, max(1024, int(ncent_main * args.fp64_fraction)))
     nat_v, clk_nat, kms_nat = timed_launches(nsub, 2)
     g.set_precision(mlipg.PREC_MIXED)
     g.set_tiling(mixed_tiling["irr_chunk"], mixed_tiling["warp_order"],

@@ -54,7 +54,7 @@ void PairMLIPGtinvGPU::allocate()
     for (int j = i; j <= n; j++) setflag[i][j] = 0;
 }
 
-// pair_style mlip_gtinv/gpu [fp64|mixed|mixed_a64]  (the reference takes no arguments,
+// pair_style mlip_gtinv/gpu [fp64|fp64_native|mixed|mixed_a64]  (the reference takes no arguments,
 // pair_mlip_gtinv_kokkos_impl.h:87-90; the optional keyword selects precision)
 void PairMLIPGtinvGPU::settings(int narg, char **arg)
 {
@@ -63,6 +63,7 @@ void PairMLIPGtinvGPU::settings(int narg, char **arg)
     if (strcmp(arg[0], "fp64") == 0) precision = MLIPG_PREC_FP64;
     else if (strcmp(arg[0], "mixed") == 0) precision = MLIPG_PREC_MIXED;
     else if (strcmp(arg[0], "mixed_a64") == 0) precision = MLIPG_PREC_MIXED_A64;
+    else if (strcmp(arg[0], "fp64_native") == 0) precision = MLIPG_PREC_FP64_NATIVE;
     else error->all(FLERR, "Illegal pair_style command");
   }
 }
