@@ -1054,16 +1054,6 @@ __device__ __forceinline__ DF pick(int z, const DF (&v)[N]) {
 }
 
 template <int N>
-__device__ __forceinline__ DFA pick_acc(int i, const DFA (&v)[N]) {
-  DFA r = v[0];
-#pragma unroll
-  for (int k = 1; k < N; ++k) {
-    r.s = (i == k) ? v[k].s : r.s;
-    r.c = (i == k) ? v[k].c : r.c;
-  }
-  return r;
-}
-template <int N>
 __device__ __forceinline__ void put_acc(int i, DFA (&v)[N], const DFA& x) {
 #pragma unroll
   for (int k = 0; k < N; ++k) {
@@ -1073,12 +1063,13 @@ __device__ __forceinline__ void put_acc(int i, DFA (&v)[N], const DFA& x) {
 }
 
 // Double-float form of run_irr (same sums, same flushes).  The loop over
-// the (z, x) element pairs is kept rolled (the operands of the current pair
-// are picked from registers by selects): fully unrolled, the double-float
-// body of one term outgrows the instruction cache and the warps wait on
-// instruction fetch.  Sums go through DFA accumulators (one FP32 add of
-// dependency per accumulation); accumulated values that are multiplied
-// again are renormalised once.
+// the z elements is kept rolled (the weights and order parameters of the
+// current z are picked from registers by selects): fully unrolled, the
+// double-float body of one term outgrows the instruction cache and the
+// warps wait on instruction fetch (rolling the (z, x) pairs as well shrinks
+// the body further but its selects cost 13 % more time).  Sums go through
+// DFA accumulators (one FP32 add of dependency per accumulation);
+// accumulated values that are multiplied again are renormalised once.
 template <int Q, int TT, int Lh, class EA>
 __device__ __forceinline__ void run_irr_df(const DeviceIrrUnit& u, const DeviceTuple* __restrict__ tups,
                                            const DeviceTerm* __restrict__ terms,
@@ -1159,69 +1150,67 @@ __device__ __forceinline__ void run_irr_df(const DeviceIrrUnit& u, const DeviceT
       cr[0] = DF(1.0f);
       ci[0] = DF(0.0f);
     }
-    // Rolled loop over the (z, x) element pairs, with m = sum_y H c_y:
-    //   S_z += b_x m,  G_x += a_z m,  G_y += H (a_z b_x)
-    // (S = sum_z a_z S_z afterwards); accumulators of the running z or x
-    // are picked and written back by selects.
     DFA gzr[NZ], gzi[NZ], gxr[NX], gxi[NX], gyr[NY], gyi[NY];
+    // Rolled loop over the z elements (x and y unrolled inside), with
+    // m[x] = sum_y H c_y:  S_z = sum_x b_x m[x],  G_x += a_z m[x],
+    // G_y += a_z sum_x H b_x; the weights of the current z are picked from
+    // registers by selects.
 #pragma unroll 1
-    for (int zx = 0; zx < NZ * NX; ++zx) {
-      const int z = zx / NX, x = zx - (zx / NX) * NX;
-      DF hz[NY];
+    for (int z = 0; z < NZ; ++z) {
+      DF Hc[NX][NY];
 #pragma unroll
-      for (int y = 0; y < NY; ++y) {
-        hz[y] = H[0][y];
-#pragma unroll
-        for (int q = 1; q < NZ * NX; ++q) hz[y] = (zx == q) ? H[q][y] : hz[y];
-      }
-      const DF bxr = pick(x, br), bxi = pick(x, bi);
-      DF mr, mi;
-      if (Q == 1) {
-        mr = hz[0];
-        mi = DF(0.0f);
-      } else {
-        DFA tr, ti;
+      for (int x = 0; x < NX; ++x)
 #pragma unroll
         for (int y = 0; y < NY; ++y) {
-          acc_fma(tr, hz[y], cr[y]);
-          acc_fma(ti, hz[y], ci[y]);
+          Hc[x][y] = H[x][y];
+#pragma unroll
+          for (int q = 1; q < NZ; ++q) Hc[x][y] = (z == q) ? H[q * NX + x][y] : Hc[x][y];
         }
-        mr = acc_val(tr);
-        mi = acc_val(ti);
-      }
-      {
-        DFA tr = pick_acc(z, gzr), ti = pick_acc(z, gzi);
-        cacc(tr, ti, bxr, bxi, mr, mi);
-        put_acc(z, gzr, tr);
-        put_acc(z, gzi, ti);
-      }
-      DFA ur = pick_acc(x, gxr), ui = pick_acc(x, gxi);
-      if (Q >= 3) {
-        const DF ar = pick(z, zr), ai = pick(z, zi);
-        cacc(ur, ui, ar, ai, mr, mi);
-        if (Q > 1) {
-          DFA pr, pi;
-          cacc(pr, pi, ar, ai, bxr, bxi);
-          const DF Pr = acc_val(pr), Pi = acc_val(pi);
+      const DF ar = pick(z, zr), ai = pick(z, zi);
+      DFA szr, szi;
+#pragma unroll
+      for (int x = 0; x < NX; ++x) {
+        DF mr, mi;
+        if (Q == 1) {
+          mr = Hc[x][0];
+          mi = DF(0.0f);
+        } else {
+          DFA tr, ti;
 #pragma unroll
           for (int y = 0; y < NY; ++y) {
-            acc_fma(gyr[y], hz[y], Pr);
-            acc_fma(gyi[y], hz[y], Pi);
+            acc_fma(tr, Hc[x][y], cr[y]);
+            acc_fma(ti, Hc[x][y], ci[y]);
           }
+          mr = acc_val(tr);
+          mi = acc_val(ti);
         }
-      } else {
-        acc_add(ur, mr);
-        acc_add(ui, mi);
-        if (Q > 1) {
+        cacc(szr, szi, br[x], bi[x], mr, mi);
+        if (Q >= 3) {
+          cacc(gxr[x], gxi[x], ar, ai, mr, mi);
+        } else {
+          acc_add(gxr[x], mr);
+          acc_add(gxi[x], mi);
+        }
+      }
+      put_acc(z, gzr, szr);
+      put_acc(z, gzi, szi);
+      if (Q > 1) {
 #pragma unroll
-          for (int y = 0; y < NY; ++y) {
-            acc_fma(gyr[y], hz[y], bxr);
-            acc_fma(gyi[y], hz[y], bxi);
+        for (int y = 0; y < NY; ++y) {
+          DFA tr, ti;
+#pragma unroll
+          for (int x = 0; x < NX; ++x) {
+            acc_fma(tr, Hc[x][y], br[x]);
+            acc_fma(ti, Hc[x][y], bi[x]);
+          }
+          if (Q >= 3) {
+            cacc(gyr[y], gyi[y], ar, ai, acc_val(tr), acc_val(ti));
+          } else {
+            gyr[y] = tr;
+            gyi[y] = ti;
           }
         }
       }
-      put_acc(x, gxr, ur);
-      put_acc(x, gxi, ui);
     }
     DF gzv_r[NZ], gzv_i[NZ];
     DFA Sr, Si;
@@ -1441,19 +1430,18 @@ __device__ __forceinline__ void radial64d(const KernelArgs& A, double r, double*
 // g0 = sum_n f_n G_n, g1 = sum_n f'_n G_n, and the same force expression as
 // ForceVis.
 struct ForceVis16 {
-  const double* g;   // Re G of the neighbour's element slot, channel 0: [Lh][16]; Im at g + gim
+  const R* g;   // Re G of the neighbour's element slot, channel 0: [Lh][16]; Im at g + gim
   int gim;
-  const double* f;
-  const double* fd;
-  double ux, uy, uz;
-  double fx, fy, fz;
-  __device__ __forceinline__ void operator()(int lmh, int mp, double yre, double yim, double xre,
-                                             double xim, double yyre, double yyim, double zre,
-                                             double zim) {
-    double g0r = 0, g0i = 0, g1r = 0, g1i = 0;
+  const R* f;
+  const R* fd;
+  R ux, uy, uz;
+  R fx, fy, fz;
+  __device__ __forceinline__ void operator()(int lmh, int mp, R yre, R yim, R xre, R xim,
+                                             R yyre, R yyim, R zre, R zim) {
+    R g0r = 0, g0i = 0, g1r = 0, g1i = 0;
 #pragma unroll
     for (int q = 0; q < kNPad; q += 4) {
-      double gr[4], gi[4];
+      R gr[4], gi[4];
       load4(g + lmh * kNPad + q, gr);
       load4(g + gim + lmh * kNPad + q, gi);
 #pragma unroll
@@ -1464,15 +1452,15 @@ struct ForceVis16 {
         g1i = fma(fd[q + k], gi[k], g1i);
       }
     }
-    const double coeff = (mp == 0) ? 1.0 : 2.0;
-    const double ry = yre * g1r + yim * g1i;
+    const R coeff = (mp == 0) ? R(1) : R(2);
+    const R ry = yre * g1r + yim * g1i;
     fx += coeff * (ry * ux + (xre * g0r + xim * g0i));
     fy += coeff * (ry * uy + (yyre * g0r + yyim * g0i));
     fz += coeff * (ry * uz + (zre * g0r + zim * g0i));
   }
 };
 
-// Column set of the FP64 force phase: column m goes to part
+// Column set of the force phase: column m goes to part
 // (0 1 2 3 3 2 1 0 0 1 ...)[m] of the four, which balances the columns'
 // lengths (L - m + 1 entries each).
 __device__ __forceinline__ int column_part(int mp) {
@@ -1480,86 +1468,89 @@ __device__ __forceinline__ int column_part(int mp) {
   return s < 4 ? s : 7 - s;
 }
 
-// sh_visit (FP64, with derivatives) restricted to the columns m of one part:
+// sh_visit (with derivatives) restricted to the columns m of one part:
 // every column still advances the cheap Q recursion that the next column's
 // derivatives read, and the angle recursions; P, Y, dY and the visitor run
 // for the part's own columns only.  `part` is uniform across the warp.
 template <int LCAP, typename V>
-__device__ __forceinline__ void sh_visit_part(double dx, double dy, double dz, double r, int L,
+__device__ __forceinline__ void sh_visit_part(R dx, R dy, R dz, R r, int L,
                                               int part, V& vis) {
-  const double invr = 1.0 / r;
-  const double ct = dz * invr;
-  const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
-  const double rho2 = dx * dx + dy * dy;
-  double cp = 1.0, sp = 0.0;
-  if (rho2 > 0.0) {
-    const double ir = 1.0 / sqrt(rho2);
+  const R invr = R(1) / r;
+  const R ct = dz * invr;
+  const R st = sqrt(fmax(R(0), R(1) - ct * ct));
+  const R rho2 = dx * dx + dy * dy;
+  R cp = R(1), sp = R(0);
+  if (rho2 > R(0)) {
+    const R ir = rsqrt_r(rho2);
     cp = dx * ir;
     sp = dy * ir;
   }
-  const double h = 0.70710678118654752440;   // 0.5 * sqrt(2)
-  double Qc[LCAP + 2];
+  constexpr bool kUnit = sizeof(R) == 4;   // FP32: Y / Y_00 (see sh_visit)
+  const R h = kUnit ? R(1) : R(0.70710678118654752440);   // 0.5 * sqrt(2)
+  R Qc[LCAP + 2];
 #pragma unroll
-  for (int l = 0; l < LCAP + 2; ++l) Qc[l] = 0.0;
-  double pdiag = 0.39894228040143267794;      // P_0^0 = sqrt(1/(2 pi))
-  double cm = 1.0, sm = 0.0, cprev = cp, sprev = -sp;
-  const double tc = 2.0 * cp;
-  double sgn = 1.0;
+  for (int l = 0; l < LCAP + 2; ++l) Qc[l] = R(0);
+  R pdiag = kUnit ? R(1) : R(0.39894228040143267794);      // P_0^0 = sqrt(1/(2 pi))
+  R cm = R(1), sm = R(0), cprev = cp, sprev = -sp;
+  const R tc = R(2) * cp;
+  R sgn = R(1);
 #pragma unroll
   for (int mp = 0; mp <= LCAP; ++mp) {
     if (mp > L) break;
     if (mp > 0) {
-      const double s = tc * sm - sprev;
-      const double c = tc * cm - cprev;
+      const R s = tc * sm - sprev;
+      const R c = tc * cm - cprev;
       cprev = cm; cm = c; sprev = sm; sm = s;
-      pdiag = pdiag * ((double)cDiag[mp] * st);
+      pdiag = pdiag * (cDiag[mp] * st);
       sgn = -sgn;
     }
     const bool mine = column_part(mp) == part;
-    const double qn_diag = (mp == 0) ? -0.48860251190291992263 : Qc[mp] * ((double)cDiag[mp + 1] * st);
-    double p1 = 0.0, p2 = 0.0, qn1 = 0.0, qn2 = 0.0;
+    // Q_1^1 = P_0^0 cDiag[1]
+    const R qn_diag = (mp == 0) ? (kUnit ? cDiag[1] : R(-0.48860251190291992263))
+                                : Qc[mp] * (cDiag[mp + 1] * st);
+    R p1 = R(0), p2 = R(0), qn1 = R(0), qn2 = R(0);
 #pragma unroll
     for (int l = mp; l <= LCAP; ++l) {
       if (l > L) break;
-      double Qn = 0.0;
+      R Qn = R(0);
       if (l == mp + 1) Qn = qn_diag;
-      else if (l == mp + 2) Qn = (ct * (double)cOff[mp + 1]) * qn1;
-      else if (l >= mp + 3) Qn = (double)cA[lm2i(l, mp + 1)] * (ct * qn1 + (double)cB[lm2i(l, mp + 1)] * qn2);
+      else if (l == mp + 2) Qn = (ct * cOff[mp + 1]) * qn1;
+      else if (l >= mp + 3) Qn = cA[lm2i(l, mp + 1)] * (ct * qn1 + cB[lm2i(l, mp + 1)] * qn2);
       if (l >= mp + 1) { qn2 = qn1; qn1 = Qn; }
       if (mine) {
-        double P;
+        R P;
         if (l == mp) P = pdiag;
-        else if (l == mp + 1) P = (ct * (double)cOff[mp]) * p1;
-        else P = (double)cA[lm2i(l, mp)] * (ct * p1 + (double)cB[lm2i(l, mp)] * p2);
+        else if (l == mp + 1) P = (ct * cOff[mp]) * p1;
+        else P = cA[lm2i(l, mp)] * (ct * p1 + cB[lm2i(l, mp)] * p2);
         p2 = p1;
         p1 = P;
-        double yre, yim;
+        R yre, yim;
         if (mp == 0) {
           yre = P * h;
-          yim = 0.0;
+          yim = R(0);
         } else {
-          const double t = sgn * P * h;
+          const R t = sgn * P * h;
           yre = t * cm;
           yim = -(t * sm);
         }
         const int lmh = l * (l + 1) / 2 + l - mp;
-        double xre = 0, xim = 0, yyre = 0, yyim = 0, zre = 0, zim = 0;
+        R xre = 0, xim = 0, yyre = 0, yyim = 0, zre = 0, zim = 0;
         if (mp == 0) {
           if (l >= 1) {
-            const double common = Qn * st * invr * (double)cLL[l];
+            const R common = Qn * st * invr * cLL[l];
             xre = common * ct * cp;
             yyre = common * ct * sp;
             zre = -common * st;
           }
         } else {
-          const double qc = Qc[l];
-          double dth = (double)mp * ct * qc;
-          if (l != mp) dth += (double)cLM[lm2i(l, mp)] * Qn * st;
-          const double dph = (double)mp * qc;
-          const double ere = cm * h * invr, eim = sm * h * invr;
-          const double vxr = dth * ct * cp, vxi = -dph * sp;
-          const double vyr = dth * ct * sp, vyi = dph * cp;
-          const double vzr = -dth * st;
+          const R qc = Qc[l];
+          R dth = R(mp) * ct * qc;
+          if (l != mp) dth += cLM[lm2i(l, mp)] * Qn * st;
+          const R dph = R(mp) * qc;
+          const R ere = cm * h * invr, eim = sm * h * invr;
+          const R vxr = dth * ct * cp, vxi = -dph * sp;
+          const R vyr = dth * ct * sp, vyi = dph * cp;
+          const R vzr = -dth * st;
           xre = sgn * (ere * vxr - eim * vxi);
           xim = -sgn * (ere * vxi + eim * vxr);
           yyre = sgn * (ere * vyr - eim * vyi);
@@ -1701,6 +1692,11 @@ __device__ __forceinline__ double nl_forward64(const DeviceUnit& u,
 }  // namespace
 
 __host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+
+// the FP64 force phase's partial forces (64 neighbours x 4 parts x 3 doubles)
+// fit the space of a of the smallest FP64 model (one element, l <= 6)
+static_assert(sizeof(R) == 4 || 28 * kNPad * sizeof(Rc) >= 64 * 4 * 3 * sizeof(double),
+              "force-phase scratch");
 
 struct SmemLayout {
   size_t a, g, dnl, hnl, nbk, misc, red, a64, total;
@@ -2265,12 +2261,14 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     double fix = 0.0, fiy = 0.0, fiz = 0.0;
     double va[6] = {0, 0, 0, 0, 0, 0};   // this centre's virial (reference order)
     if constexpr (sizeof(R) == 8) {
-      // FP64 kernels: 32 neighbours per warp, the four warps of a group split
-      // the m columns of the harmonics (each Y_lm and dY_lm computed once, all
-      // 16 channels contracted per entry); the four partial forces of a
-      // neighbour meet in shared memory (the space of a in the all-FP64
-      // kernel, of the adjoint words in the double-float one: neither is read
-      // again for this centre) and are added in a fixed order.
+      // FP64 kernels: 32 neighbours per warp; the four warps of a group
+      // split the m columns of the harmonics (each Y_lm and dY_lm computed
+      // once, all 16 channels contracted per entry); the four partial forces
+      // of a neighbour meet in shared memory (the space of a, at least 7 KB,
+      // or of the adjoint words in the double-float kernel: neither is read
+      // again for this centre) and are added in a fixed order.  (The FP32
+      // form of this split measured 6.6 % slower on the mixed kernel: its
+      // 16 channels do not fit the register budget of two CTAs per SM.)
       double* pf = reinterpret_cast<double*>(kDF ? static_cast<void*>(sg) : static_cast<void*>(sa));
       const int part = warp & 3, grp = warp >> 2;
       const int rounds = (nkeep + 2 * 32 - 1) / (2 * 32);
@@ -2288,13 +2286,13 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
         double f[kNPad], fd[kNPad];
         radial64d(A, r, f, fd);
         const double ir = 1.0 / r;
-        ForceVis16 v{reinterpret_cast<const double*>(gP6) + (size_t)tj * LS * kNPad, gim, f, fd,
-                     dx * ir, dy * ir, dz * ir, 0.0, 0.0, 0.0};
-        sh_visit_part<LCAP>(dx, dy, dz, r, L, part, v);
+        ForceVis16 v{gP6 + (size_t)tj * LS * kNPad, gim, f, fd, (R)(dx * ir), (R)(dy * ir),
+                     (R)(dz * ir), R(0), R(0), R(0)};
+        sh_visit_part<LCAP>((R)dx, (R)dy, (R)dz, (R)r, L, part, v);
         double* q = pf + ((grp * 32 + lane) * 4 + part) * 3;
-        q[0] = v.fx;
-        q[1] = v.fy;
-        q[2] = v.fz;
+        q[0] = (double)v.fx;
+        q[1] = (double)v.fy;
+        q[2] = (double)v.fz;
         __syncthreads();
         if (part == 0 && valid) {
           const double* q0 = pf + (grp * 32 + lane) * 12;
