@@ -1468,11 +1468,11 @@ __device__ __forceinline__ int column_part(int mp) {
   return s < 4 ? s : 7 - s;
 }
 
-// sh_visit (with derivatives) restricted to the columns m of one part:
-// every column still advances the cheap Q recursion that the next column's
-// derivatives read, and the angle recursions; P, Y, dY and the visitor run
-// for the part's own columns only.  `part` is uniform across the warp.
-template <int LCAP, typename V>
+// sh_visit restricted to the columns m of one part: every column still
+// advances the angle recursions and (with DERIV) the cheap Q recursion that
+// the next column's derivatives read; P, Y, dY and the visitor run for the
+// part's own columns only.  `part` is uniform across the warp.
+template <int LCAP, typename V, bool DERIV = true>
 __device__ __forceinline__ void sh_visit_part(R dx, R dy, R dz, R r, int L,
                                               int part, V& vis) {
   const R invr = R(1) / r;
@@ -1506,17 +1506,20 @@ __device__ __forceinline__ void sh_visit_part(R dx, R dy, R dz, R r, int L,
     }
     const bool mine = column_part(mp) == part;
     // Q_1^1 = P_0^0 cDiag[1]
-    const R qn_diag = (mp == 0) ? (kUnit ? cDiag[1] : R(-0.48860251190291992263))
-                                : Qc[mp] * (cDiag[mp + 1] * st);
+    const R qn_diag = !DERIV ? R(0)
+                      : (mp == 0) ? (kUnit ? cDiag[1] : R(-0.48860251190291992263))
+                                  : Qc[mp] * (cDiag[mp + 1] * st);
     R p1 = R(0), p2 = R(0), qn1 = R(0), qn2 = R(0);
 #pragma unroll
     for (int l = mp; l <= LCAP; ++l) {
       if (l > L) break;
       R Qn = R(0);
-      if (l == mp + 1) Qn = qn_diag;
-      else if (l == mp + 2) Qn = (ct * cOff[mp + 1]) * qn1;
-      else if (l >= mp + 3) Qn = cA[lm2i(l, mp + 1)] * (ct * qn1 + cB[lm2i(l, mp + 1)] * qn2);
-      if (l >= mp + 1) { qn2 = qn1; qn1 = Qn; }
+      if (DERIV) {
+        if (l == mp + 1) Qn = qn_diag;
+        else if (l == mp + 2) Qn = (ct * cOff[mp + 1]) * qn1;
+        else if (l >= mp + 3) Qn = cA[lm2i(l, mp + 1)] * (ct * qn1 + cB[lm2i(l, mp + 1)] * qn2);
+        if (l >= mp + 1) { qn2 = qn1; qn1 = Qn; }
+      }
       if (mine) {
         R P;
         if (l == mp) P = pdiag;
@@ -1535,6 +1538,10 @@ __device__ __forceinline__ void sh_visit_part(R dx, R dy, R dz, R r, int L,
         }
         const int lmh = l * (l + 1) / 2 + l - mp;
         R xre = 0, xim = 0, yyre = 0, yyim = 0, zre = 0, zim = 0;
+        if (!DERIV) {
+          vis(lmh, mp, yre, yim, xre, xim, yyre, yyim, zre, zim);
+          continue;
+        }
         if (mp == 0) {
           if (l >= 1) {
             const R common = Qn * st * invr * cLL[l];
@@ -1560,7 +1567,7 @@ __device__ __forceinline__ void sh_visit_part(R dx, R dy, R dz, R r, int L,
         }
         vis(lmh, mp, yre, yim, xre, xim, yyre, yyim, zre, zim);
       }
-      if (l >= mp + 1) Qc[l] = Qn;
+      if (DERIV && l >= mp + 1) Qc[l] = Qn;
     }
   }
 }
@@ -1937,18 +1944,30 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       const int b0 = misc[t], b1 = misc[t + 1];
       for (int cb = b0; cb < b1; cb += kChunk) {
         const int csz = min(kChunk, b1 - cb);
-        if (tid < csz) {
-          const int k = nbk[cb + tid];
+        // staging by four warps: neighbour = lane, the warps split the
+        // harmonic columns (warp 0 also the radial functions)
+        const int slot = tid & 31, part = tid >> 5;
+        if (part < 4 && slot < csz) {
+          const int k = nbk[cb + slot];
           const int j = __ldg(A.nbr_idx + k);
           double dx, dy, dz;
           pair_disp(A, c, k, xi, A.x4[j], dx, dy, dz);
           const double r = sqrt(dx * dx + dy * dy + dz * dz);
-          R f[kNPad], fdum[kNPad];
-          radial(A.radial, F, (R)r, rc, f, fdum, false);
+          if (part == 0) {
+            if constexpr (sizeof(R) == 8) {
+              double f64[kNPad];
+              radial64(A, r, f64);
 #pragma unroll
-          for (int n = 0; n < kNPad; ++n) fs[tid * kNPad + n] = (double)f[n];
-          StageVis v{ys, tid};
-          sh_visit<LCAP, false>((R)dx, (R)dy, (R)dz, (R)r, L, v);
+              for (int n = 0; n < kNPad; ++n) fs[slot * kNPad + n] = f64[n];
+            } else {   // mixed path with FP64 sums: FP32 radial functions
+              R f[kNPad], fdum[kNPad];
+              radial(A.radial, F, (R)r, rc, f, fdum, false);
+#pragma unroll
+              for (int n = 0; n < kNPad; ++n) fs[slot * kNPad + n] = (double)f[n];
+            }
+          }
+          StageVis v{ys, slot};
+          sh_visit_part<LCAP, StageVis, false>((R)dx, (R)dy, (R)dz, (R)r, L, part, v);
         }
         __syncthreads();
 #pragma unroll
