@@ -1716,7 +1716,10 @@ __host__ __device__ inline SmemLayout smem_layout(int T, int Lh, int nb_cap, int
   // adjoint: FP64 re/im, the mixed path's int32 high + low parts of re/im,
   // or the double-float path's four int32 words of re/im
   const size_t gn = (size_t)T * Lh * kNPad * (4 * kGWords);
-  const size_t stage = (size_t)Lh * kChunk * sizeof(double2) + (size_t)kChunk * kNPad * sizeof(double);
+  // neighbour staging; with FP64 l = 0 inputs (lh64 == 1) the mixed
+  // path's window also stages their FP64 radial functions (64 x 16 doubles)
+  const size_t stage = (size_t)Lh * kChunk * sizeof(double2) + (size_t)kChunk * kNPad * sizeof(double) +
+                       (lh64 == 1 ? (size_t)2 * kChunk * kNPad * sizeof(double) : 0);
   s.a = 0;
   s.g = align16(an);
   s.dnl = s.g + align16(gn > stage ? gn : stage);
@@ -1888,9 +1891,19 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       // bytes of the FP64 one), across element boundaries, so one window
       // usually holds the whole neighbourhood; an element that spans windows
       // carries its rounded sum from the previous window.
+      // With the polynomial's FP64 inputs at l = 0 alone (lh64 == 1, the
+      // model_type 3 case), their FP64 order parameters a64[t][n] =
+      // Y_00 sum_j f_n(r_j) are made in the same windows: the staging thread
+      // also evaluates the FP64 radial functions and T x 16 threads sum them
+      // (the order and the sums of order_params64, without its second pass
+      // over the neighbours).
       constexpr int kWin = 2 * kChunk;
       float2* ysf = reinterpret_cast<float2*>(sg);
       float* fsf = reinterpret_cast<float*>(smem + lay.g + (size_t)LS * kWin * sizeof(float2));
+      double* fs64 = reinterpret_cast<double*>(smem + lay.g + (size_t)LS * kWin * sizeof(float2) +
+                                               (size_t)kWin * kNPad * sizeof(float));
+      const bool fuse64 = A.lh64 == 1 && __ldg(A.nl_off + ti + 1) > __ldg(A.nl_off + ti);
+      double acc64 = 0.0;   // thread t * 16 + n: element t, channel n
       const int n = tid & 15;
       for (int w0 = 0; w0 < nkeep; w0 += kWin) {
         const int wsz = min(kWin, nkeep - w0);
@@ -1900,6 +1913,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           double dx, dy, dz;
           pair_disp(A, c, k, xi, A.x4[j], dx, dy, dz);
           const double r = sqrt(dx * dx + dy * dy + dz * dz);
+          if (fuse64) {
+            double f64[kNPad];
+            radial64(A, r, f64);
+#pragma unroll
+            for (int q = 0; q < kNPad; ++q) fs64[tid * kNPad + q] = f64[q];
+          }
           R f[kNPad], fdum[kNPad];
           radial(A.radial, F, (R)r, rc, f, fdum, false);
 #pragma unroll
@@ -1908,6 +1927,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
           sh_visit<LCAP, false>((R)dx, (R)dy, (R)dz, (R)r, L, v);
         }
         __syncthreads();
+        if (fuse64 && tid < T * kNPad) {
+          const int t64 = tid >> 4;
+          const int j0 = max(misc[t64], w0), j1 = min(misc[t64 + 1], w0 + wsz);
+          for (int jj = j0 - w0; jj < j1 - w0; ++jj) acc64 += fs64[jj * kNPad + n];
+        }
         for (int t = 0; t < T; ++t) {
           const int j0 = max(misc[t], w0), j1 = min(misc[t + 1], w0 + wsz);
           if (j0 >= j1) continue;
@@ -1936,6 +1960,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
       for (int t = 0; t < T; ++t)   // elements without neighbours
         if (misc[t] == misc[t + 1])
           for (int idx = tid; idx < Lh * kNPad; idx += kBlock) sa[t * LS * kNPad + idx] = Rc{R(0), R(0)};
+      if (fuse64 && tid < T * kNPad)   // Y_00 = sqrt(1 / (4 pi)), real
+        reinterpret_cast<double2*>(smem + lay.a64)[tid] = double2{0.28209479177387814347 * acc64, 0.0};
     } else
     for (int t = 0; t < T; ++t) {
       double accr[kEPT], acci[kEPT];
@@ -2003,7 +2029,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) fused_kernel(const __grid_
     // sum to, so their inputs must carry FP64 accuracy; for model_type 3
     // these are the l = 0 entries alone.
     if constexpr (sizeof(R) == 4) {
-      if (A.lh64 > 0 && nNL > 0) {
+      // (made in P2's windows when lh64 == 1 and P2 summed in FP32)
+      const bool in_p2 = LCAP <= 16 && !A.sum64 && A.lh64 == 1;
+      if (A.lh64 > 0 && nNL > 0 && !in_p2) {
         __syncthreads();   // the staging of P2 (same space) is no longer read
         order_params64(A, c, xi, misc, nbk, reinterpret_cast<double2*>(sg), a64);
       }
