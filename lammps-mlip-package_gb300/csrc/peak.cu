@@ -1,5 +1,6 @@
-// FP32 / FP64 FMA throughput microkernels.  The fused MLIP kernel is bound by
-// the CUDA-core FP32 (mixed path) or FP64 (plain path) pipes, whose peaks are
+// FP32 / FP64 FMA throughput microkernels.  The fused MLIP kernels are bound
+// by the CUDA-core FP32 pipe (mixed and double-float kernels) or the FP64 pipe
+// (the all-FP64 kernel), whose peaks are
 // not among the copy / tensor-core peaks measured for the machine; these
 // kernels measure them live on the same device so the roofline fraction has
 // a measured denominator.

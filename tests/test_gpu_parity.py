@@ -313,3 +313,24 @@ def test_device_api_totals_match_per_atom(potdir, ncent):
     v = out.cpu().numpy()[1:7]
     # kernel order xx yy zz yz zx xy vs oracle's LAMMPS order xx yy zz xy xz yz
     np.testing.assert_allclose(v[[0, 1, 2, 5, 4, 3]], ref["virial"], rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("prec", [mlipg.PREC_FP64, mlipg.PREC_FP64_NATIVE])
+def test_sparse_neighbourhoods(tmp_path, prec):
+    """Dilute random cells (0.004 atoms per cubic angstrom: a few neighbours
+    each, mostly near the cutoff) make the order parameters, and with them
+    the adjoint flushes, orders of magnitude smaller than in a dense cell:
+    the double-float kernel's fixed-point scale adapts to them (and caps at
+    2^100) without leaving FP64 parity."""
+    p = str(tmp_path / "sparse.mlip")
+    workload_potential(p, "triclinic-batch", seed=6)
+    g = mlipg.Potential(p, prec)
+    o = Oracle(p, threads=8)
+    rng = np.random.default_rng(21)
+    for n in (6, 20):
+        cell = random_triclinic_cell(n, 0.004, 2, rng, min_dist=3.0)
+        s = build_system(cell, o.cutoff, skin=1.0)
+        got = g.compute(s)
+        check_fp64(got, o.compute(s), s)
+        assert g.device_status() == 0
+    g.close()
