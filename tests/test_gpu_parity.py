@@ -334,3 +334,40 @@ def test_sparse_neighbourhoods(tmp_path, prec):
         check_fp64(got, o.compute(s), s)
         assert g.device_status() == 0
     g.close()
+
+
+SINGLE_TUPLE = {
+    # more than three elements: every irreps runs one element tuple per unit
+    "4el-order3": dict(elements=["A", "B", "C", "D"], maxl=4, order=3, gtinv_maxl=[4, 2]),
+    # orders 5 and 6 (the table's l <= 1 terms): single-tuple units beside the
+    # batched ones of orders <= 4
+    "2el-order6": dict(elements=["A", "B"], maxl=4, order=6, gtinv_maxl=[4, 2, 2, 1, 1]),
+}
+
+
+@pytest.mark.parametrize("spec", sorted(SINGLE_TUPLE))
+def test_single_tuple_units(tmp_path, spec):
+    """The single-tuple units (run_unit: any order up to 6, any number of
+    elements) in every precision: FP64 and all-FP64 against the oracle at
+    1e-10, mixed within the stated bounds."""
+    from mlipg.potential import gaussian_params, write_potential
+    h = SINGLE_TUPLE[spec]
+    path = str(tmp_path / (spec + ".mlip"))
+    ne = len(h["elements"])
+    write_potential(path, h["elements"], 5.0, gaussian_params(6, 5.0), 3, 2, h["maxl"],
+                    h["order"], h["gtinv_maxl"], [0] * (h["order"] - 1),
+                    masses=[27.0] * ne, seed=13)
+    rng = np.random.default_rng(17)
+    cell = random_types(jitter(fcc_cell(2, 2, 2, 3.6), 0.05, rng), ne, rng)
+    o = Oracle(path, threads=16)
+    s = build_system(cell, o.cutoff, skin=1.0)
+    ref = o.compute(s)
+    for prec in (mlipg.PREC_FP64, mlipg.PREC_FP64_NATIVE):
+        g = mlipg.Potential(path, prec)
+        check_fp64(g.compute(s), ref, s)
+        assert g.device_status() == 0
+        g.close()
+    mix = mlipg.Potential(path, mlipg.PREC_MIXED).compute(s)
+    F, Fr = s.fold_forces(mix["f_all"]), s.fold_forces(ref["f_all"])
+    assert np.sqrt(np.mean((F - Fr) ** 2)) <= 1e-4
+    assert abs(mix["energy"] - ref["energy"]) <= mixed_energy_bound(o, s)
