@@ -67,6 +67,10 @@ WORKLOADS = {
     # step a CUDA graph
     "md-fcc-al-256": dict(kind="md", lattice="fcc", n=4, a=4.05, ntypes=1, jitter=0.05,
                           pot="fcc-al-256", temperature=300.0, dt=0.001),
+    # 16,000-atom binary bcc at 300 K (run it with --steps 100): the same NVE run in
+    # mixed and in FP64 precision, each step a CUDA graph
+    "md-bcc-binary-16k": dict(kind="md", lattice="bcc", n=20, a=3.2, ntypes=2, jitter=0.05,
+                              pot="bcc-binary-16k", temperature=300.0, dt=0.001, fp64=True),
     # 50 NVE steps of the 1M-atom ternary alloy at 300 K, each step a CUDA graph
     "md-fcc-ternary-1m": dict(kind="md", lattice="fcc", n=64, a=4.0, ntypes=3, jitter=0.1,
                               pot="fcc-ternary-1m", temperature=300.0, dt=0.001),
@@ -923,10 +927,37 @@ def run_md(args, dist):
     el = time.perf_counter() - t0
     clk = clocks.stop()
     th1 = md.thermo()
+    x_mixed = md.state()[0]
     el = replicas.max_over_ranks(el, dist)
     n = cell.natoms
     value = n * args.steps * dist["world"] / el
-    nb = 4 * 4.0 / 3.0 * np.pi * 6.0 ** 3 / spec["a"] ** 3
+    fp64_rec = None
+    if spec.get("fp64"):
+        # the same run (cell, velocities, warm-up and timed steps) in FP64
+        g64 = mlipg.Potential(pot, mlipg.PREC_FP64)
+        md64 = mlipg.MD(g64, cell, v, skin=SKIN)
+        md64.run(args.warmup, spec["dt"], True)
+        th0_64 = md64.thermo()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        md64.run(args.steps, spec["dt"], True)
+        torch.cuda.synchronize()
+        el64 = replicas.max_over_ranks(time.perf_counter() - t0, dist)
+        th1_64 = md64.thermo()
+        d = x_mixed - md64.state()[0]
+        fr = d @ np.linalg.inv(cell.lattice)
+        d = (fr - np.round(fr)) @ cell.lattice     # minimum image
+        md64.close()
+        g64.close()
+        v64 = n * args.steps * dist["world"] / el64
+        fp64_rec = {"value": v64, "unit": UNIT, "ms_per_step": el64 / args.steps * 1e3,
+                    "what": "MLIPG_PREC_FP64 (double-float invariant/adjoint products)",
+                    "energy_drift_eV_per_atom": (th1_64["etotal"] - th0_64["etotal"]) / n,
+                    "mixed_over_fp64": value / v64,
+                    "mixed_vs_fp64_max_displacement_A": float(np.abs(d).max()),
+                    "mixed_vs_fp64_pe_eV_per_atom": abs(th1["pe"] - th1_64["pe"]) / n}
+    per_cell = 4 if spec["lattice"] == "fcc" else 2   # atoms per conventional cell
+    nb = per_cell * 4.0 / 3.0 * np.pi * 6.0 ** 3 / spec["a"] ** 3
     flops = type_flops(g, [cell.types], nb)
     peak = mlipg.measure_fma_peak(False)
     ach = flops / (el / args.steps) / 1e12
@@ -953,6 +984,7 @@ def run_md(args, dist):
                 "roofline": {"bound": "fp32-cuda-core", "achieved": ach, "peak": peak,
                              "unit": "TFLOP/s", "frac": ach / peak, "traffic": None,
                              "note": "whole MD step time (upper bound of the force kernel)"},
+                "fp64": fp64_rec,
                 "cpu_baseline": None, "clocks": clk,
                 # per step one graph of 5 kernels (first half-kick, fused force kernel,
                 # finalize, second half-kick, displacement check); list rebuilds
