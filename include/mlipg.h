@@ -130,9 +130,9 @@ int mlipg_compute(mlipg_handle* h, int nlocal, int nall, const double* x, const 
  *     holds the launch's status bits as a double (0 = clean; 1: an atom had
  *     more neighbours inside the cutoff than nb_cap, its energy and forces
  *     were skipped; 2: an element index outside the potential's elements;
- *     4: mixed path, adjoint outside the fixed-point range).  The call only
- *     enqueues work: read d_out8[7] after synchronising the stream, or call
- *     mlipg_device_status.
+ *     4: mixed or double-float path, adjoint outside the fixed-point
+ *     range).  The call only enqueues work: read d_out8[7] after
+ *     synchronising the stream, or call mlipg_device_status.
  * No counterpart in the reference (its device stages are internal,
  * mlipkk_lmp.h:145-228); this is the entry used by MD loops and batching. */
 int mlipg_compute_device(mlipg_handle* h, int ncenters, const void* d_x4, const int* d_centers,
@@ -167,7 +167,7 @@ void* mlipg_stream(mlipg_handle* h);
 
 /* Status bits of the handle's last fused-kernel launch (any entry point):
  * waits for the handle's stream, then reads the launch's status word
- * (1 neighbour capacity, 2 element index, 4 mixed-path adjoint range; the
+ * (1 neighbour capacity, 2 element index, 4 fixed-point adjoint range; the
  * same value as that launch's d_out8[7]).  MD runs, batches and served
  * requests check the word themselves and fail with MLIPG_ECAPACITY,
  * MLIPG_EINVAL or MLIPG_ENOTSUP. */

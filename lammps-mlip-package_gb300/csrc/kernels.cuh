@@ -15,7 +15,7 @@ constexpr int kLhMax = (kMaxL + 1) * (kMaxL + 2) / 2;
 enum StatusBits : int {
   kStatusNeighbourCapacity = 1,  // an atom had more neighbours inside rc than nb_cap
   kStatusBadType = 2,            // an element index outside [0, T) in the inputs
-  kStatusAdjointRange = 4,       // mixed path: adjoint flushes out of the fixed-point range
+  kStatusAdjointRange = 4,       // fixed-point paths: adjoint flushes out of the range
 };
 
 struct KernelArgs {
