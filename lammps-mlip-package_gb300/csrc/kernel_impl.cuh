@@ -6,13 +6,14 @@
 //   P1  neighbour compaction: keep r <= rc, stable-sort by element (all
 //       warps, per-warp counts and a prefix keep the list order)
 //   P2  order parameters a[s][lm][n] = sum_j f_n(r) conj(Y_lm): f_n and Y_lm
-//       evaluated in REAL; FP64 path (and the mixed precision that asks
-//       for FP64 sums): staged as FP64 and summed with FP64 FMAs; mixed
-//       path: FP32 products summed with Kahan compensation
-//       (mlipkk_lmp.h:314-387, mlipkk_features_kk.h:9-48,
-//       mlipkk_spherical_harmonics_kk.h:18-81)
+//       evaluated in REAL; FP64 kernels (and the mixed precision that asks
+//       for FP64 sums): staged as FP64 by four warps that split the
+//       harmonic columns, summed with FP64 FMAs; mixed path: FP32 products
+//       summed with Kahan compensation (mlipkk_lmp.h:314-387,
+//       mlipkk_features_kk.h:9-48, mlipkk_spherical_harmonics_kk.h:18-81)
 //   P2b mixed path: the order parameters that the polynomial's input
-//       features read, in FP64 (FP64 radial functions, Y_lm and sums)
+//       features read, in FP64 (FP64 radial functions, Y_lm and sums; the
+//       l = 0 rows inside P2's windows)
 //   P3  the polynomial's input features ("nonlinear" features, in FP64) and
 //       their whole energy: linear terms and polynomial terms of order >= 2,
 //       and H = dE/dd for them (mlipkk_lmp.h:489-625)
@@ -21,7 +22,9 @@
 //       (mlipkk_lmp.h:407-469, 645-733)
 //   P6  per-pair forces f_ij = sum coeff Re(G . dphi*) with the centre's own
 //       adjoint, scattered as F_i += f, F_j -= f; virial -= r_ij (x) f
-//       (mlipkk_lmp.h:753-922, spherical-harmonic derivatives :117-177)
+//       (mlipkk_lmp.h:753-922, spherical-harmonic derivatives :117-177);
+//       FP64 kernels split the harmonic columns over four warps, the mixed
+//       path the 16 radial channels over four threads per neighbour
 // The "owner computes" force form: a pair's other half comes from the
 // neighbour's own evaluation (identical to the reference's j<i / ghost
 // split up to summation order).
