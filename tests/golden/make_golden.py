@@ -131,7 +131,9 @@ def model_fingerprint(L, path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <reference package root (with test/regression)>")
+    ref = sys.argv[1]
     reg = os.path.join(ref, "test", "regression")
     sys.path.insert(0, os.path.join(REPO, "lammps-mlip-package_gb300"))
     from mlipg.structures import read_lammps_data
