@@ -3,7 +3,7 @@
 Run in an environment where the reference sources are present (they are not
 on the GPU host; the outputs of this script are committed):
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference
 
 What it writes:
 * ``gtinv-{197,820,434}.mlip.gz``, ``pair-{60,17}.mlip.gz`` -- the
