@@ -3,11 +3,12 @@
 Each request's result in the mix (many requests in flight, FP64 and mixed
 interleaved) equals the same structure evaluated alone: energies to 1e-13
 relative (they are reduced per cell in a fixed order), forces and virials to
-1e-12 of the force / virial scale in FP64 (only the order of the FP64 force
-scatter differs) and 1e-7 in the mixed path: its adjoint sums are exact
-fixed point, but the fixed-point scale adapts from the centres a CTA ran
-before, which depend on the batch, and each FP32 flush is rounded to
-2^-31 .. 2^-37 of the CTA's largest flush (measured differences up to 1.2e-8
+1e-12 of the force / virial scale in FP64 and 1e-7 in the mixed path.  Both
+accumulate the adjoint in exact fixed point whose scale adapts from the
+centres a CTA ran before, which depend on the batch: the FP64 precision's
+double-float flushes are rounded 64 bits below the CTA's largest flush (far
+below FP64 rounding; the FP64 force scatter's order differs too), the mixed
+path's FP32 flushes 31 .. 37 bits below it (measured differences up to 1.2e-8
 of the force scale, below the 6e-8 rounding of the FP32 products
 themselves).
 """
