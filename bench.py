@@ -569,6 +569,11 @@ def run_ours(args, dist):
         line["batch_4096"] = batch_record(sub, SOLO, "triclinic-batch-4096")
         sub.requests = 2000
         line["serving"] = serve_record(sub, SOLO, "serve-poisson")
+        # the NVE configurations: 100 steps of the 256-atom cell, and 100 steps
+        # of the 16K binary in mixed and FP64
+        sub.steps, sub.warmup = 100, 3
+        line["md_256"] = md_record(sub, SOLO, "md-fcc-al-256")
+        line["md_16k"] = md_record(sub, SOLO, "md-bcc-binary-16k")
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -899,11 +904,17 @@ def serve_record(args, dist, workload):
 
 def run_md(args, dist):
     """NVE molecular dynamics (velocity Verlet), each step one CUDA graph."""
+    line = md_record(args, dist, args.workload)
+    if dist["rank"] == 0:
+        print(json.dumps(line), flush=True)
+
+
+def md_record(args, dist, workload):
     import torch
 
     import mlipg
     from mlipg.potential import workload_potential
-    spec = WORKLOADS[args.workload]
+    spec = WORKLOADS[workload]
     rank = dist["rank"]
     tmp = tempfile.mkdtemp()
     pot = os.path.join(tmp, "pot.mlip")
@@ -968,7 +979,7 @@ def run_md(args, dist):
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": args.workload, "atoms": n,
+                "config": {"workload": workload, "atoms": n,
                            "potential": POT_DESC[spec["pot"]],
                            "md": "NVE velocity Verlet, dt %.3f ps, %g K Maxwell-Boltzmann, "
                                  "skin %.1f A, list rebuilt when an atom moves skin/2"
@@ -992,7 +1003,8 @@ def run_md(args, dist):
                 "gpu_launches": 5 * args.steps,
                 "graph_launches": args.steps,
                 "list_rebuilds": int(th1["rebuilds"] - th0["rebuilds"])}
-        print(json.dumps(line), flush=True)
+        return line
+    return None
 
 
 def main():
