@@ -272,7 +272,7 @@ void mlipg_dnlist_destroy(mlipg_dnlist* L);
  * Results agree between tilings to rounding (the energy summation is grouped
  * by unit).  mlipg_set_tiling waits for the handle's stream and re-uploads the
  * schedules; MD objects re-capture their step graph afterwards.
- * mlipg_autotune times every candidate (irr_chunk 12/24/48 x the three orders x
+ * mlipg_autotune times every candidate (irr_chunk 12/24/48/96 x the three orders x
  * 1..resident CTAs/SM) on up to 16 centres per resident CTA of the given
  * structure (same arguments as mlipg_compute_device), keeps the fastest and
  * writes rows [irr_chunk, warp_order, ctas_per_sm, ms] to report (up to

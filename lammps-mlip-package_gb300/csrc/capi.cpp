@@ -934,7 +934,7 @@ extern "C" int mlipg_autotune(mlipg_handle* h, int ncenters, const void* d_x4,
   CK(cudaEventCreate(&e0), "event create");
   CK(cudaEventCreate(&e1), "event create");
   int rc = MLIPG_OK;
-  for (int chunk : {12, 24, 48})
+  for (int chunk : {12, 24, 48, 96})
     for (int order : {0, 1, 2})
       for (int cps = 1; cps <= bps_max && rc == MLIPG_OK; ++cps) {
         rc = mlipg_set_tiling(h, chunk, order, cps);
